@@ -1,0 +1,181 @@
+/*
+ * smip_gpu.h -- C ABI of the GB300 speckle-masking (SMIP) engine.
+ *
+ * libsmip_gpu.so replaces the hot path of hangeza/speckle-stacker v0.3.2
+ * (per-frame FFT + power spectrum, bispectrum accumulation, cross-correlation
+ * shift-and-add, closure-phase recovery, final reconstruction).  All entry
+ * points are extern "C", take plain pointers and sizes, return an int status
+ * (SMIP_OK = 0) and leave a thread-local message for smip_last_error().
+ * The C++ layer in speckle-stacker_gb300/include/smip/ maps the status codes
+ * back to the exception types the reference throws.
+ *
+ * Conventions (the reference's own):
+ *   - 2-D arrays are ncols x nrows, row-major, x fastest; spectra, phases and
+ *     power spectra are in FFT order (negative frequencies wrapped by +size,
+ *     include/array2.h:310-339).
+ *   - complex values are interleaved (re, im): complex<float> bispectrum
+ *     (include/types.h:33), complex<double> phases/images (types.h:32).
+ *   - the bispectrum is the reference's packed half-space array, base_size =
+ *     (ncols/2+1)(nrows+1)(d/2+1)(d+1) elements, d = bdepth rounded down to
+ *     even (include/bispectrum.h:203-220, 324-349).
+ *
+ * Every call is asynchronous on the object's CUDA stream unless it returns
+ * host data; host-data calls synchronise that stream first.
+ */
+#ifndef SMIP_GPU_H
+#define SMIP_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SMIP_GPU_API __attribute__((visibility("default")))
+#else
+#define SMIP_GPU_API
+#endif
+
+/* ---- status codes (mirroring the reference's exception types) ------------ */
+#define SMIP_OK 0
+#define SMIP_E_INVALID_ARGUMENT 1 /* std::invalid_argument (crosscorrel.h:100-102, bispectrum.h:235-237) */
+#define SMIP_E_OUT_OF_RANGE 2     /* std::out_of_range (bispectrum.h:491-507, array2.h:274-306) */
+#define SMIP_E_RUNTIME 3          /* std::runtime_error (I/O bispectrum.h:418-459, /0 array_base.h:342-344) */
+#define SMIP_E_DOMAIN 4           /* std::domain_error (window aperture <= 0, window_function.h:20) */
+#define SMIP_E_BAD_CALL 5         /* std::bad_function_call (correlation not ready, crosscorrel.h:149-159) */
+#define SMIP_E_NO_MEMORY 6        /* device allocation failed or admission budget exceeded */
+#define SMIP_E_CUDA 7             /* CUDA runtime error */
+#define SMIP_E_TIMEOUT 8          /* a bounded device-side wait expired (kernel returned early) */
+#define SMIP_E_UNSUPPORTED 9      /* shape outside what the GPU kernels implement */
+
+/* ---- frame element types ------------------------------------------------- */
+#define SMIP_U8 0
+#define SMIP_U16 1
+#define SMIP_F32 2
+#define SMIP_F64 3
+
+typedef struct smip_stack* smip_stack_t;
+
+/* Message for the last failing call on this thread ("" if none). */
+SMIP_GPU_API const char* smip_last_error(void);
+
+/* Library version; the reference's is config/config.h:40-46 (0.3.2). */
+SMIP_GPU_API int smip_version(int* major, int* minor, int* patch);
+
+/* ========================================================================== *
+ * Stack: one speckle-masking job.  Owns the device-resident accumulators of
+ * smip-cli/main.cpp:232-312 -- packed bispectrum plus Kahan compensation
+ * (Bispectrum<complex<float>>, main.cpp:253), power spectrum (main.cpp:274-279,
+ * 300-305), shift-and-add sum (main.cpp:263-266, 293-294), the cross
+ * correlation reference (frame 0, main.cpp:268) and the frame count.
+ * ========================================================================== */
+
+/* Replaces Bispectrum<complex<float>>({ncols, nrows, bdepth, bdepth})
+ * (bispectrum.h:183-192, main.cpp:253) plus the accumulators above.
+ * stream: a cudaStream_t to run on, or NULL for a stream owned by the stack.
+ * batch_frames: frames per accumulation batch (0 = library default).
+ * Supported: ncols, nrows powers of two in [16, 1024]; bdepth/2*2 a multiple
+ * of 8 in [8, 64] and < min(ncols, nrows). */
+SMIP_GPU_API int smip_stack_create(smip_stack_t* out, int device, long ncols, long nrows,
+                                   long bdepth, void* stream, long batch_frames);
+SMIP_GPU_API int smip_stack_destroy(smip_stack_t s);
+
+/* Replaces the per-frame body of smip-cli/main.cpp:281-306 (and 247-279 for
+ * the stack's first frame): cross-correlate against frame 0 (crosscorrel.h:
+ * 181-189), add the back-shifted frame to the sum (array2.h:603-622), forward
+ * FFT (main.cpp:296), accumulate the bispectrum (bispectrum.h:356-409) and the
+ * power spectrum.  frames: count frames of ncols x nrows elements of dtype,
+ * consecutive frames frame_stride_bytes apart (0 = tightly packed); on_device
+ * non-zero if the pointer is device memory.  Host buffers are read before the
+ * call returns unless they are page-locked, in which case they must stay
+ * unchanged until smip_stack_sync. */
+SMIP_GPU_API int smip_stack_push_frames(smip_stack_t s, const void* frames, int dtype, long count,
+                                        long frame_stride_bytes, int on_device);
+
+/* Replaces Bispectrum::accumulate_from_fft(const Array2<complex<double>>&)
+ * (bispectrum.h:82-83, 356-409) for spectra computed elsewhere: count spectra
+ * of ncols x nrows complex<double> in FFT order, host or device memory.
+ * Only the bispectrum is accumulated (no power spectrum or shift-and-add). */
+SMIP_GPU_API int smip_stack_accumulate_fft(smip_stack_t s, const double* spectra, long count, int on_device);
+
+/* Runs the pending partial batch; smip_stack_sync also waits for it. */
+SMIP_GPU_API int smip_stack_flush(smip_stack_t s);
+SMIP_GPU_API int smip_stack_sync(smip_stack_t s);
+
+SMIP_GPU_API int smip_stack_frame_count(smip_stack_t s, long* nframes);
+SMIP_GPU_API int smip_stack_bispectrum_size(smip_stack_t s, long* base_size);
+
+/* Integer shift-and-add shifts of frames [first, first+count): (x, y) pairs
+ * as CrossCorrelation::operator() returns them (crosscorrel.h:166-179);
+ * frame 0 is the reference and reports (0, 0). */
+SMIP_GPU_API int smip_stack_shifts(smip_stack_t s, int* xy, long first, long count);
+
+/* Normalised results of main.cpp:307-312, copied to host:
+ * sum: ncols*nrows doubles (sumarray / nframes);
+ * power: ncols*nrows doubles (real part of powerspec / (nframes*ncols*nrows));
+ * bispec: 2*base_size floats (bispectrum / nframes, the bispectrum.dat payload). */
+SMIP_GPU_API int smip_stack_sum(smip_stack_t s, double* sum);
+SMIP_GPU_API int smip_stack_power(smip_stack_t s, double* power);
+SMIP_GPU_API int smip_stack_bispectrum(smip_stack_t s, float* bispec);
+
+/* Replaces reconstruct_phases<complex_t, complex<float>>(bispectrum, ncols,
+ * nrows, reco_radius, &pm) (phasereco.h:16-19, 33-123) on the stack's
+ * normalised bispectrum.  phases: ncols*nrows complex<double>; flags and
+ * consistency: the PhaseMap (phasemap.h:10-18), ncols*nrows each.  Any
+ * output pointer may be NULL.  SMIP_E_OUT_OF_RANGE where the reference's
+ * Bispectrum::get_element would throw. */
+SMIP_GPU_API int smip_stack_reconstruct(smip_stack_t s, double reco_radius, double* phases,
+                                        unsigned char* flags, double* consistency);
+
+/* Replaces main.cpp:318-376 as a whole: phase reconstruction, Hann window of
+ * aperture 2*reco_radius (window_function.h:39-46, main.cpp:329-330),
+ * sqrt(power) x phases, backward FFT and division by the largest modulus.
+ * image: ncols*nrows complex<double> (may be NULL); phases/flags/consistency
+ * as above (pre-window phases, as reconstruct_phases returns them). */
+SMIP_GPU_API int smip_stack_finish(smip_stack_t s, double reco_radius, double* image, double* phases,
+                                   unsigned char* flags, double* consistency);
+
+/* Adds src's accumulators into dst (same shape): frame-level sharding of one
+ * stack across accumulators (the accumulation is additive).  dst keeps its
+ * own reference frame; src must have been created after dst received its
+ * first frame and with dst as reference (smip_stack_share_reference). */
+SMIP_GPU_API int smip_stack_merge(smip_stack_t dst, smip_stack_t src);
+/* Makes src correlate against dst's reference frame (frame 0 of dst). */
+SMIP_GPU_API int smip_stack_share_reference(smip_stack_t dst, smip_stack_t src);
+
+/* Bispectrum::write_to_file / read_from_file (bispectrum.h:411-462): the
+ * normalised bispectrum in the reference's bispectrum.dat format. */
+SMIP_GPU_API int smip_stack_save_bispectrum(smip_stack_t s, const char* path);
+
+/* ========================================================================== *
+ * Standalone calls mirroring the reference's free functions and classes.
+ * ========================================================================== */
+
+/* reconstruct_phases on a host Bispectrum<complex<float>> (phasereco.h:16-19).
+ * bispec: 2*base_size floats for (xsize, ysize, bdepth). */
+SMIP_GPU_API int smip_reconstruct_phases(int device, const float* bispec, long xsize, long ysize, long bdepth,
+                                         double reco_radius, double* phases, unsigned char* flags,
+                                         double* consistency);
+
+/* NextRecoIndex (phasereco.h:21, phasereco.cpp:17-36); host arithmetic. */
+SMIP_GPU_API int smip_next_reco_index(double* r, double* phi, int* i, int* j);
+
+/* Number of visits of the reconstruction loop for reco_radius and, when
+ * ij != NULL, the visited (i, j) pairs (phasereco.h:56-68); host arithmetic. */
+SMIP_GPU_API int smip_reco_visits(double reco_radius, int* ij, long cap, long* count);
+
+/* CrossCorrelation<double>::get_displacement(ref, frame) (crosscorrel.h:54-58)
+ * on the GPU: ref and frame are ncols x nrows doubles (host).  corr (may be
+ * NULL) receives the unnormalised correlation array (crosscorrel.h:147-152). */
+SMIP_GPU_API int smip_xcorr_displacement(int device, const double* ref, const double* frame, long ncols,
+                                         long nrows, int* dx, int* dy, double* corr);
+
+/* Hann<double>(xsize, ysize, aperture) (window_function.h:39-46, 70-85),
+ * computed on the GPU; SMIP_E_DOMAIN for aperture <= 0. */
+SMIP_GPU_API int smip_hann(int device, double* out, long xsize, long ysize, double aperture);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SMIP_GPU_H */

@@ -1,0 +1,274 @@
+// k_fft.cu -- per-frame forward FFT (FP32, shared memory), power spectrum and
+// the cross-correlation transforms.
+//
+// Replaces the FFTW calls of smip-cli/main.cpp:256-259, 271, 296 (forward
+// c2c of each frame), the |F|^2 accumulation of main.cpp:274-279, 300-305 and
+// the r2c / c2r pair of CrossCorrelation::correlate (include/crosscorrel.h:
+// 103-141).  Frames are real, so only the u_x <= 0 half plane is computed;
+// the other half is its complex conjugate mirror.
+//
+// Layout written for the bispectrum kernel (per frame, float2):
+//   S[a][c] = F(x = -a, y = c - H/2),  a in [0, W/2], c in [0, H)
+// i.e. rows indexed by -u_x (the reference's packed dim 0, bispectrum.h:327)
+// and y centred, so every tile the bispectrum kernel needs is one rectangular
+// TMA box, with zero fill exactly where the reference's loop bounds stop
+// (bispectrum.h:397-398).
+#include "smip_dev.cuh"
+
+namespace smip_gpu {
+
+template <typename T> __device__ __forceinline__ float pix_f(const T* p, long long i) { return (float)p[i]; }
+
+// ---------------------------------------------------------------- row pass
+// Two real rows per complex FFT of length W (x0 + i x1); the half-spectra are
+// separated afterwards.  Output G'(a, y) = sum_x f(x, y) exp(+2 pi i a x / W).
+template <typename T>
+__global__ void __launch_bounds__(256) row_pass_kernel(const T* __restrict__ frames, long long fstride, int logW, int H,
+                                                        int hw, float2* __restrict__ Gt, const float2* __restrict__ tw_g)
+{
+    extern __shared__ float2 sm[];
+    float2* tw = sm;                              // 2^(kTwLog-1)
+    float2* lines = sm + (1 << (kTwLog - 1));     // [kRowBlock/2][W]
+    const int W = 1 << logW;
+    const int f = blockIdx.y;
+    const int y0 = blockIdx.x * kRowBlock;
+    const T* fr = frames + (long long)f * fstride + (long long)y0 * W;
+    load_twiddles(tw, tw_g, kTwLog);
+    for (int idx = threadIdx.x; idx < kRowBlock * W; idx += blockDim.x) {
+        const int r = idx >> logW, x = idx & (W - 1);
+        const float v = pix_f(fr, idx);
+        float* dst = reinterpret_cast<float*>(&lines[(r >> 1) * W + bitrev(x, logW)]);
+        dst[r & 1] = v;
+    }
+    __syncthreads();
+    fft_stages(lines, logW, kRowBlock / 2, W, tw, kTwLog, -1);
+    float2* out = Gt + (long long)f * hw * H;
+    for (int idx = threadIdx.x; idx < hw * kRowBlock; idx += blockDim.x) {
+        const int a = idx / kRowBlock, r = idx - a * kRowBlock;
+        const float2* Z = lines + (r >> 1) * W;
+        const float2 za = Z[a], zb = Z[(W - a) & (W - 1)];
+        float2 g;
+        if ((r & 1) == 0) // conj of X0 = (Z(a) + conj Z(-a)) / 2
+            g = make_float2(0.5f * (za.x + zb.x), -0.5f * (za.y - zb.y));
+        else // conj of X1 = (Z(a) - conj Z(-a)) / 2i
+            g = make_float2(0.5f * (za.y + zb.y), 0.5f * (za.x - zb.x));
+        out[(long long)a * H + y0 + r] = g;
+    }
+}
+
+// ------------------------------------------------------------- column pass
+// One CTA per (a, chunk of frames).  Forward FFT along y gives
+// Fm(a, y) = F(-a, y); writes S, accumulates |F|^2 in FP64 (frame order), and
+// for the correlation computes the inverse y-transform of conj(R) * Fm in
+// place of the input column.
+__global__ void __launch_bounds__(256) col_pass_kernel(int mode, float2* __restrict__ Gt, float2* __restrict__ S,
+                                                        const float2* __restrict__ Rbuf, float2* __restrict__ Rout,
+                                                        double* __restrict__ Ppart, int nframes, int fpc,
+                                                        int skip_xcorr_frame0, int logH, int hw,
+                                                        const float2* __restrict__ tw_g)
+{
+    extern __shared__ float2 sm[];
+    const int H = 1 << logH;
+    float2* tw = sm;
+    float2* R = tw + (1 << (kTwLog - 1));          // [H]
+    float2* L1 = R + H;                            // [kColLines][H]
+    float2* L2 = L1 + kColLines * H;               // [kColLines][H]
+    double* pacc = reinterpret_cast<double*>(L2 + kColLines * H); // [H]
+    const int a = blockIdx.x;
+    const int chunk = blockIdx.y;
+    const int fbeg = chunk * fpc;
+    const int fend = min(nframes, fbeg + fpc);
+    const long long gstride = (long long)hw * H;
+    load_twiddles(tw, tw_g, kTwLog);
+    if (mode == 0)
+        for (int y = threadIdx.x; y < H; y += blockDim.x) {
+            R[y] = Rbuf[(long long)a * H + y];
+            pacc[y] = 0.0;
+        }
+    for (int f0 = fbeg; f0 < fend; f0 += kColLines) {
+        const int nl = min(kColLines, fend - f0);
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nl * H; idx += blockDim.x) {
+            const int l = idx >> logH, y = idx & (H - 1);
+            L1[l * H + bitrev(y, logH)] = Gt[(f0 + l) * gstride + (long long)a * H + y];
+        }
+        __syncthreads();
+        fft_stages(L1, logH, nl, H, tw, kTwLog, -1);
+        if (mode == 1) { // reference spectrum only
+            for (int y = threadIdx.x; y < H; y += blockDim.x)
+                Rout[(long long)a * H + y] = L1[y];
+            return;
+        }
+        for (int idx = threadIdx.x; idx < nl * H; idx += blockDim.x) {
+            const int l = idx >> logH, c = idx & (H - 1);
+            S[(f0 + l) * gstride + (long long)a * H + c] = L1[l * H + ((c + H / 2) & (H - 1))];
+        }
+        // power spectrum, frames in order per element
+        for (int c = threadIdx.x; c < H; c += blockDim.x) {
+            double acc = pacc[c];
+            for (int l = 0; l < nl; ++l) {
+                const float2 v = L1[l * H + ((c + H / 2) & (H - 1))];
+                acc += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+            }
+            pacc[c] = acc;
+        }
+        // correlation product conj(R) * F, bit-reversed for the inverse FFT
+        for (int idx = threadIdx.x; idx < nl * H; idx += blockDim.x) {
+            const int l = idx >> logH, y = idx & (H - 1);
+            const float2 r = R[y], v = L1[l * H + y];
+            L2[l * H + bitrev(y, logH)] = make_float2(r.x * v.x + r.y * v.y, r.x * v.y - r.y * v.x);
+        }
+        __syncthreads();
+        fft_stages(L2, logH, nl, H, tw, kTwLog, +1);
+        for (int idx = threadIdx.x; idx < nl * H; idx += blockDim.x) {
+            const int l = idx >> logH, y = idx & (H - 1);
+            if (skip_xcorr_frame0 && f0 + l == 0)
+                continue;
+            Gt[(f0 + l) * gstride + (long long)a * H + y] = L2[l * H + y];
+        }
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < H; c += blockDim.x)
+        Ppart[(long long)chunk * gstride + (long long)a * H + c] = pacc[c];
+}
+
+__global__ void power_reduce_kernel(double* __restrict__ P, const double* __restrict__ Ppart, int nchunks, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double acc = P[i];
+        for (int c = 0; c < nchunks; ++c)
+            acc += Ppart[(long long)c * n + i];
+        P[i] = acc;
+    }
+}
+
+// ------------------------------------------------------- correlation rows
+// c2r along x of T(-a, y): Hermitian extension Z(k) = T(a=k)* for 0<k<W/2,
+// T(a=W-k) for k>W/2, real parts at k = 0, W/2 (as FFTW's c2r ignores those
+// imaginary parts); two rows per complex FFT.  Output: unnormalised
+// correlation c[y][x] = W*H * sum ref(p) frame(p + (x,y)).
+__global__ void __launch_bounds__(256) xcorr_rows_kernel(const float2* __restrict__ Gt, float* __restrict__ corr,
+                                                          int logW, int H, int hw, const float2* __restrict__ tw_g)
+{
+    extern __shared__ float2 sm[];
+    const int W = 1 << logW;
+    float2* tw = sm;
+    float2* Ts = tw + (1 << (kTwLog - 1));         // [hw][kRowBlock]
+    float2* lines = Ts + hw * kRowBlock;           // [kRowBlock/2][W]
+    const int f = blockIdx.y;
+    const int y0 = blockIdx.x * kRowBlock;
+    const float2* T = Gt + (long long)f * hw * H;
+    load_twiddles(tw, tw_g, kTwLog);
+    for (int idx = threadIdx.x; idx < hw * kRowBlock; idx += blockDim.x) {
+        const int a = idx / kRowBlock, r = idx - a * kRowBlock;
+        Ts[idx] = T[(long long)a * H + y0 + r];
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < (kRowBlock / 2) * W; idx += blockDim.x) {
+        const int p = idx >> logW, k = idx & (W - 1);
+        float2 z[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int r = 2 * p + h;
+            if (k == 0)
+                z[h] = make_float2(Ts[0 * kRowBlock + r].x, 0.f);
+            else if (k < W / 2)
+                z[h] = cconj(Ts[k * kRowBlock + r]);
+            else if (k == W / 2)
+                z[h] = make_float2(Ts[(W / 2) * kRowBlock + r].x, 0.f);
+            else
+                z[h] = Ts[(W - k) * kRowBlock + r];
+        }
+        lines[p * W + bitrev(k, logW)] = make_float2(z[0].x - z[1].y, z[0].y + z[1].x);
+    }
+    __syncthreads();
+    fft_stages(lines, logW, kRowBlock / 2, W, tw, kTwLog, +1);
+    float* out = corr + (long long)f * W * H + (long long)y0 * W;
+    for (int idx = threadIdx.x; idx < kRowBlock * W; idx += blockDim.x) {
+        const int r = idx >> logW, x = idx & (W - 1);
+        const float2 v = lines[(r >> 1) * W + x];
+        out[idx] = (r & 1) ? v.y : v.x;
+    }
+}
+
+// ----------------------------------------------------- spectrum import
+// FFT-order complex<double> spectra (ncols x nrows) -> S layout (float2).
+__global__ void import_spectra_kernel(const double2* __restrict__ in, int nframes, int W, int H, int hw,
+                                      float2* __restrict__ S)
+{
+    const long long per = (long long)hw * H;
+    const long long n = per * nframes;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long f = i / per;
+        const int rem = (int)(i - f * per);
+        const int a = rem / H, c = rem - a * H;
+        const int x = (W - a) & (W - 1);
+        const int y = (c + H / 2) & (H - 1);
+        const double2 v = in[f * (long long)W * H + (long long)y * W + x];
+        S[i] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
+// ------------------------------------------------------------- launchers
+static int grid_for(long long n, int block)
+{
+    long long g = (n + block - 1) / block;
+    return (int)(g > 4096 ? 4096 : (g < 1 ? 1 : g));
+}
+
+cudaError_t launch_row_pass(int dtype, const void* frames, long long fstride, int nframes, const Geometry& g,
+                            float2* Gt, const float2* tw, cudaStream_t st)
+{
+    const dim3 grid(g.H / kRowBlock, nframes);
+    const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + (kRowBlock / 2) * g.W);
+    switch (dtype) {
+    case 0: row_pass_kernel<uint8_t><<<grid, 256, smem, st>>>((const uint8_t*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); break;
+    case 1: row_pass_kernel<uint16_t><<<grid, 256, smem, st>>>((const uint16_t*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); break;
+    case 2: row_pass_kernel<float><<<grid, 256, smem, st>>>((const float*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); break;
+    default: row_pass_kernel<double><<<grid, 256, smem, st>>>((const double*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_col_pass(int mode, float2* Gt, float2* S, const float2* Rbuf, float2* Rout, double* Ppart,
+                            int nframes, int fpc, int skip_xcorr_frame0, const Geometry& g, const float2* tw,
+                            cudaStream_t st)
+{
+    const int nchunks = mode == 1 ? 1 : (nframes + fpc - 1) / fpc;
+    const dim3 grid(g.hw, nchunks);
+    const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + g.H + 2 * kColLines * g.H) + sizeof(double) * g.H;
+    col_pass_kernel<<<grid, 256, smem, st>>>(mode, Gt, S, Rbuf, Rout, Ppart, mode == 1 ? 1 : nframes, fpc,
+                                             skip_xcorr_frame0, g.logH, g.hw, tw);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_power_reduce(double* P, const double* Ppart, int nchunks, const Geometry& g, cudaStream_t st)
+{
+    const long long n = (long long)g.hw * g.H;
+    power_reduce_kernel<<<grid_for(n, 256), 256, 0, st>>>(P, Ppart, nchunks, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_xcorr_rows(const float2* Gt, float* corr, int nframes, const Geometry& g, const float2* tw,
+                              cudaStream_t st)
+{
+    const dim3 grid(g.H / kRowBlock, nframes);
+    const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + g.hw * kRowBlock + (kRowBlock / 2) * g.W);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(xcorr_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
+    }
+    xcorr_rows_kernel<<<grid, 256, smem, st>>>(Gt, corr, g.logW, g.H, g.hw, tw);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_import_spectra(const double* spectra, int nframes, const Geometry& g, float2* S, cudaStream_t st)
+{
+    const long long n = (long long)g.hw * g.H * nframes;
+    import_spectra_kernel<<<grid_for(n, 256), 256, 0, st>>>(reinterpret_cast<const double2*>(spectra), nframes, g.W,
+                                                             g.H, g.hw, S);
+    return cudaGetLastError();
+}
+
+} // namespace smip_gpu

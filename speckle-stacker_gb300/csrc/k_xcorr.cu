@@ -1,0 +1,235 @@
+// k_xcorr.cu -- integer shift of each frame against frame 0, and the
+// shift-and-add sum.
+//
+// Replaces CrossCorrelation::calculate_displacement (include/crosscorrel.h:
+// 166-179: first maximum of the FP64 FFT correlation in row-major order,
+// wrapped to a signed shift) and the sumarray update of smip-cli/main.cpp:
+// 289-294 with Array2::shifted (include/array2.h:603-622).
+//
+// The correlation arrives in FP32 (k_fft.cu).  Every position within an
+// error bound of the FP32 peak is re-scored exactly -- integer arithmetic for
+// u8/u16 frames, FP64 for float frames -- and the best exact value wins, ties
+// to the lowest linear index (std::max_element's first maximum).  The bound
+// is 8 * 2^-24 * log2(W*H) * ||ref||_2 * ||frame||_2 * W*H, a few times the
+// worst-case error of an FP32 radix-2 FFT convolution.
+#include "smip_dev.cuh"
+
+namespace smip_gpu {
+
+constexpr int kShiftThreads = 512;
+constexpr int kMaxCand = 1024;
+
+template <typename T> struct ExactAcc { using type = double; };
+template <> struct ExactAcc<uint8_t> { using type = unsigned long long; };
+template <> struct ExactAcc<uint16_t> { using type = unsigned long long; };
+
+template <typename A>
+__device__ A block_sum(A v, A* red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0)
+        red[w] = v;
+    __syncthreads();
+    A s = 0;
+    for (int i = 0; i < nw; ++i)
+        s += red[i];
+    return s;
+}
+
+template <typename A, typename T> __device__ __forceinline__ A mul_exact(T a, T b) { return (A)a * (A)b; }
+template <> __device__ __forceinline__ unsigned long long mul_exact<unsigned long long, uint16_t>(uint16_t a, uint16_t b)
+{
+    return (unsigned long long)((unsigned)a * (unsigned)b); // < 2^32, exact
+}
+template <> __device__ __forceinline__ unsigned long long mul_exact<unsigned long long, uint8_t>(uint8_t a, uint8_t b)
+{
+    return (unsigned long long)((unsigned)a * (unsigned)b);
+}
+
+template <typename T>
+__device__ typename ExactAcc<T>::type exact_corr(const T* ref, const T* fr, int W, int H, int sx, int sy,
+                                                 typename ExactAcc<T>::type* red)
+{
+    using A = typename ExactAcc<T>::type;
+    A acc = 0;
+    for (int p = threadIdx.x; p < W * H; p += blockDim.x) {
+        const int x = p & (W - 1), y = p / W;
+        const int xs = (x + sx) & (W - 1), ys = (y + sy) & (H - 1);
+        acc += mul_exact<A>(ref[p], fr[ys * W + xs]);
+    }
+    return block_sum(acc, red);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float* __restrict__ corr,
+                                                                     const T* __restrict__ frames, long long fstride,
+                                                                     const T* __restrict__ ref, const double* ref_sq,
+                                                                     int first_is_frame0, int W, int H,
+                                                                     int* __restrict__ shifts)
+{
+    using A = typename ExactAcc<T>::type;
+    __shared__ A redA[32];
+    __shared__ double redD[32];
+    __shared__ float redF[32];
+    __shared__ int cand[kMaxCand];
+    __shared__ int ncand;
+    const int f = blockIdx.x;
+    if (first_is_frame0 && f == 0) {
+        if (threadIdx.x == 0) {
+            shifts[0] = 0;
+            shifts[1] = 0;
+        }
+        return;
+    }
+    const int n = W * H;
+    const float* c = corr + (long long)f * n;
+    const T* fr = frames + (long long)f * fstride;
+    // ||frame||^2 and the FP32 peak
+    double sq = 0.0;
+    float mx = -INFINITY;
+    for (int p = threadIdx.x; p < n; p += blockDim.x) {
+        const double v = (double)fr[p];
+        sq += v * v;
+        mx = fmaxf(mx, c[p]);
+    }
+    sq = block_sum(sq, redD);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0)
+        redF[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    mx = redF[0];
+    for (int i = 1; i < (int)(blockDim.x >> 5); ++i)
+        mx = fmaxf(mx, redF[i]);
+    const double tau = 8.0 * 5.9604644775390625e-08 * (double)(__ffs(n) - 1) * sqrt(*ref_sq * sq) * (double)n;
+    const float thr = (float)((double)mx - tau);
+
+    A best = 0;
+    int best_idx = -1;
+    if (threadIdx.x == 0)
+        ncand = 0;
+    __syncthreads();
+    // Windows of blockDim.x positions; the candidate list is re-scored and
+    // emptied whenever the next window would overflow it, so every position
+    // with c >= thr is re-scored exactly once.
+    auto flush = [&]() {
+        const int nc = ncand;
+        for (int q = 0; q < nc; ++q) {
+            const int p = cand[q];
+            const A v = exact_corr(ref, fr, W, H, p & (W - 1), p / W, redA);
+            if (best_idx < 0 || v > best || (v == best && p < best_idx)) {
+                best = v;
+                best_idx = p;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            ncand = 0;
+        __syncthreads();
+    };
+    for (int base = 0; base < n; base += blockDim.x) {
+        const int p = base + threadIdx.x;
+        const bool hit = p < n && c[p] >= thr;
+        const int wc = __syncthreads_count(hit);
+        if (wc == 0)
+            continue;
+        if (ncand + wc > kMaxCand)
+            flush();
+        if (hit)
+            cand[atomicAdd(&ncand, 1)] = p;
+        __syncthreads();
+    }
+    flush();
+    if (threadIdx.x == 0) {
+        int sx = best_idx & (W - 1), sy = best_idx / W;
+        sx -= (sx < (W + 1) / 2) ? 0 : W;
+        sy -= (sy < (H + 1) / 2) ? 0 : H;
+        shifts[2 * f] = sx;
+        shifts[2 * f + 1] = sy;
+    }
+}
+
+__device__ __forceinline__ unsigned long long abs_px(unsigned long long v) { return v; }
+__device__ __forceinline__ double abs_px(double v) { return fabs(v); }
+
+// sum[y][x] += |frame[y + sy][x + sx]| where inside the frame, frames in
+// order (main.cpp:293-294); the stack's frame 0 enters unshifted with its
+// sign (main.cpp:266).
+template <typename T, typename A>
+__global__ void saa_add_kernel(A* __restrict__ sum, const T* __restrict__ frames, long long fstride, int nframes,
+                               int first_is_frame0, const int* __restrict__ shifts, int W, int H)
+{
+    const int n = W * H;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const int x = p & (W - 1), y = p / W;
+        A acc = sum[p];
+        for (int f = 0; f < nframes; ++f) {
+            const int xs = x + shifts[2 * f], ys = y + shifts[2 * f + 1];
+            if (xs >= 0 && xs < W && ys >= 0 && ys < H) {
+                const A v = (A)frames[(long long)f * fstride + ys * W + xs];
+                acc += (first_is_frame0 && f == 0) ? v : abs_px(v);
+            }
+        }
+        sum[p] = acc;
+    }
+}
+
+template <typename T>
+__global__ void sumsq_kernel(const T* __restrict__ fr, long long n, double* out)
+{
+    __shared__ double red[32];
+    double s = 0.0;
+    for (long long p = threadIdx.x; p < n; p += blockDim.x) {
+        const double v = (double)fr[p];
+        s += v * v;
+    }
+    s = block_sum(s, red);
+    if (threadIdx.x == 0)
+        *out = s;
+}
+
+cudaError_t launch_xcorr_shift(int dtype, const float* corr, const void* frames, long long fstride, const void* ref,
+                               const double* ref_sq, int nframes, int first_is_frame0, const Geometry& g, int* shifts,
+                               cudaStream_t st)
+{
+    switch (dtype) {
+    case 0: xcorr_shift_kernel<uint8_t><<<nframes, kShiftThreads, 0, st>>>(corr, (const uint8_t*)frames, fstride, (const uint8_t*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); break;
+    case 1: xcorr_shift_kernel<uint16_t><<<nframes, kShiftThreads, 0, st>>>(corr, (const uint16_t*)frames, fstride, (const uint16_t*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); break;
+    case 2: xcorr_shift_kernel<float><<<nframes, kShiftThreads, 0, st>>>(corr, (const float*)frames, fstride, (const float*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); break;
+    default: xcorr_shift_kernel<double><<<nframes, kShiftThreads, 0, st>>>(corr, (const double*)frames, fstride, (const double*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_saa_add(int dtype, void* sum, const void* frames, long long fstride, int nframes,
+                           int first_is_frame0, const int* shifts, const Geometry& g, cudaStream_t st)
+{
+    const int n = g.W * g.H;
+    const int grid = (n + 255) / 256;
+    switch (dtype) {
+    case 0: saa_add_kernel<uint8_t, unsigned long long><<<grid, 256, 0, st>>>((unsigned long long*)sum, (const uint8_t*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); break;
+    case 1: saa_add_kernel<uint16_t, unsigned long long><<<grid, 256, 0, st>>>((unsigned long long*)sum, (const uint16_t*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); break;
+    case 2: saa_add_kernel<float, double><<<grid, 256, 0, st>>>((double*)sum, (const float*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); break;
+    default: saa_add_kernel<double, double><<<grid, 256, 0, st>>>((double*)sum, (const double*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sumsq(int dtype, const void* frame, long long n, double* out, cudaStream_t st)
+{
+    switch (dtype) {
+    case 0: sumsq_kernel<uint8_t><<<1, 1024, 0, st>>>((const uint8_t*)frame, n, out); break;
+    case 1: sumsq_kernel<uint16_t><<<1, 1024, 0, st>>>((const uint16_t*)frame, n, out); break;
+    case 2: sumsq_kernel<float><<<1, 1024, 0, st>>>((const float*)frame, n, out); break;
+    default: sumsq_kernel<double><<<1, 1024, 0, st>>>((const double*)frame, n, out); break;
+    }
+    return cudaGetLastError();
+}
+
+} // namespace smip_gpu

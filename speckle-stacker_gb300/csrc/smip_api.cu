@@ -1,0 +1,905 @@
+// smip_api.cu -- host runtime behind the C ABI (include/smip_gpu.h).
+//
+// A stack owns the device-resident accumulators of one speckle-masking job
+// and runs the per-frame pipeline in batches on its CUDA stream:
+//
+//   raw frames -> row FFT -> column FFT (S, |F|^2, correlation columns)
+//              -> correlation rows -> integer shifts -> shift-and-add
+//              -> bispectrum accumulation over the whole batch
+//
+// Only the final reconstruction steps (phase recovery, image) and result
+// downloads synchronise the stream.  The spiral visit list of
+// NextRecoIndex is host arithmetic (phasereco.cpp:17-36), computed once per
+// radius and uploaded.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/smip_gpu.h"
+#include "smip_internal.h"
+
+using namespace smip_gpu;
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                                     \
+    do {                                                                                                   \
+        cudaError_t e_ = (expr);                                                                           \
+        if (e_ != cudaSuccess)                                                                             \
+            return fail(e_ == cudaErrorMemoryAllocation ? SMIP_E_NO_MEMORY : SMIP_E_CUDA,                  \
+                        std::string(#expr) + ": " + cudaGetErrorString(e_));                               \
+    } while (0)
+
+extern "C" const char* smip_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int smip_version(int* major, int* minor, int* patch)
+{
+    if (major) *major = 0;
+    if (minor) *minor = 3;
+    if (patch) *patch = 2;
+    return SMIP_OK;
+}
+
+// ---------------------------------------------------------- device context
+namespace {
+
+struct DeviceCtx {
+    float2* tw32 = nullptr;  // exp(-2 pi i k / 2^kTwLog), k < 2^(kTwLog-1)
+    double2* tw64 = nullptr;
+    int num_sms = 0;
+};
+
+std::mutex g_ctx_mu;
+std::map<int, DeviceCtx> g_ctx;
+
+int device_ctx(int dev, DeviceCtx** out)
+{
+    std::lock_guard<std::mutex> lk(g_ctx_mu);
+    auto it = g_ctx.find(dev);
+    if (it == g_ctx.end()) {
+        DeviceCtx c;
+        CUDA_TRY(cudaSetDevice(dev));
+        CUDA_TRY(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, dev));
+        const int n = 1 << (kTwLog - 1);
+        std::vector<float2> t32(n);
+        std::vector<double2> t64(n);
+        for (int k = 0; k < n; ++k) {
+            const double a = 2.0 * M_PI * (double)k / (double)(1 << kTwLog);
+            t64[k] = make_double2(std::cos(a), -std::sin(a));
+            t32[k] = make_float2((float)t64[k].x, (float)t64[k].y);
+        }
+        CUDA_TRY(cudaMalloc(&c.tw32, sizeof(float2) * n));
+        CUDA_TRY(cudaMalloc(&c.tw64, sizeof(double2) * n));
+        CUDA_TRY(cudaMemcpy(c.tw32, t32.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(c.tw64, t64.data(), sizeof(double2) * n, cudaMemcpyHostToDevice));
+        it = g_ctx.emplace(dev, c).first;
+    }
+    *out = &it->second;
+    return SMIP_OK;
+}
+
+int ilog2(long v)
+{
+    int l = 0;
+    while ((1L << l) < v)
+        ++l;
+    return l;
+}
+
+bool pow2(long v) { return v > 0 && (v & (v - 1)) == 0; }
+
+size_t dtype_size(int dt)
+{
+    switch (dt) {
+    case SMIP_U8: return 1;
+    case SMIP_U16: return 2;
+    case SMIP_F32: return 4;
+    case SMIP_F64: return 8;
+    default: return 0;
+    }
+}
+
+int make_geometry(long W, long H, long bdepth, Geometry* g)
+{
+    if (!pow2(W) || !pow2(H) || W < 16 || H < 16 || W > (1 << kMaxLog) || H > (1 << kMaxLog))
+        return fail(SMIP_E_UNSUPPORTED, "frame size must be a power of two in [16, 512] per axis");
+    const int De = (int)(bdepth / 2) * 2;
+    if (bdepth < 0)
+        return fail(SMIP_E_INVALID_ARGUMENT, "bdepth must be non-negative");
+    if (!bispec_depth_supported(De))
+        return fail(SMIP_E_UNSUPPORTED, "bispectrum depth (rounded down to even) must be a multiple of 8 in [8, 64]");
+    if (De >= W || De >= H)
+        return fail(SMIP_E_UNSUPPORTED, "bispectrum depth must be smaller than the frame size");
+    g->W = (int)W;
+    g->H = (int)H;
+    g->logW = ilog2(W);
+    g->logH = ilog2(H);
+    g->hw = (int)W / 2 + 1;
+    g->De = De;
+    g->E = (De / 2 + 1) * (De + 1);
+    g->base_size = (long long)g->hw * (H + 1) * g->E;
+    return SMIP_OK;
+}
+
+// phasereco.cpp:17-36, the reference's own host arithmetic
+void next_reco_index(double& r, double& phi, int& i, int& j)
+{
+    const double dr = 1.0;
+    const double dphi = 1.0 / (2.0 * M_PI * r);
+    int ii = i, jj = j;
+    while ((i == ii) && (j == jj)) {
+        if ((phi += dphi) > 2.0 * M_PI) {
+            phi = 0;
+            r += dr;
+        }
+        ii = static_cast<int>(r * std::cos(phi));
+        jj = static_cast<int>(r * std::sin(phi));
+    }
+    i = ii;
+    j = jj;
+}
+
+// phasereco.h:56-68
+std::vector<int2> reco_visits(double R)
+{
+    std::vector<int2> v;
+    double r = 0.0, phi = 0.0;
+    int i = 0, j = 0;
+    while (r <= R) {
+        next_reco_index(r, phi, i, j);
+        v.push_back(make_int2(i, j));
+    }
+    return v;
+}
+
+template <typename T> void dfree(T*& p)
+{
+    if (p)
+        cudaFree(p);
+    p = nullptr;
+}
+
+// Buffers of one phase reconstruction.
+struct Reco {
+    Geometry g {};
+    double R = -1.0;
+    int2* visits = nullptr;
+    int nvisits = 0;
+    double2* phases = nullptr;
+    float2* phf = nullptr;
+    double* cons = nullptr;
+    unsigned char* flags = nullptr;
+    RecoJob* job = nullptr;
+    ~Reco()
+    {
+        dfree(visits);
+        dfree(phases);
+        dfree(phf);
+        dfree(cons);
+        dfree(flags);
+        dfree(job);
+    }
+    int run(const float2* Bnorm, double radius, int* err, cudaStream_t st)
+    {
+        const size_t np = (size_t)g.W * g.H;
+        if (!phases) {
+            CUDA_TRY(cudaMalloc(&phases, sizeof(double2) * np));
+            CUDA_TRY(cudaMalloc(&phf, sizeof(float2) * np));
+            CUDA_TRY(cudaMalloc(&cons, sizeof(double) * np));
+            CUDA_TRY(cudaMalloc(&flags, np));
+            CUDA_TRY(cudaMalloc(&job, sizeof(RecoJob)));
+        }
+        if (radius != R) {
+            std::vector<int2> v = reco_visits(radius);
+            dfree(visits);
+            CUDA_TRY(cudaMalloc(&visits, sizeof(int2) * v.size()));
+            CUDA_TRY(cudaMemcpyAsync(visits, v.data(), sizeof(int2) * v.size(), cudaMemcpyHostToDevice, st));
+            nvisits = (int)v.size();
+            R = radius;
+        }
+        CUDA_TRY(cudaMemsetAsync(phases, 0, sizeof(double2) * np, st));
+        CUDA_TRY(cudaMemsetAsync(phf, 0, sizeof(float2) * np, st));
+        CUDA_TRY(cudaMemsetAsync(cons, 0, sizeof(double) * np, st));
+        RecoJob j;
+        j.B = Bnorm;
+        j.visits = visits;
+        j.nvisits = nvisits;
+        j.W = g.W;
+        j.H = g.H;
+        j.De = g.De;
+        j.phases = phases;
+        j.phf = phf;
+        j.cons = cons;
+        j.flags = flags;
+        j.err = err;
+        CUDA_TRY(cudaMemcpyAsync(job, &j, sizeof(RecoJob), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(launch_phase_reco(job, 1, g.W, g.H, st));
+        return SMIP_OK;
+    }
+    int download(double* ph, unsigned char* fl, double* cs, cudaStream_t st)
+    {
+        const size_t np = (size_t)g.W * g.H;
+        if (ph)
+            CUDA_TRY(cudaMemcpyAsync(ph, phases, sizeof(double2) * np, cudaMemcpyDeviceToHost, st));
+        if (fl)
+            CUDA_TRY(cudaMemcpyAsync(fl, flags, np, cudaMemcpyDeviceToHost, st));
+        if (cs)
+            CUDA_TRY(cudaMemcpyAsync(cs, cons, sizeof(double) * np, cudaMemcpyDeviceToHost, st));
+        return SMIP_OK;
+    }
+};
+
+int check_dev_err(int* err_dev, cudaStream_t st)
+{
+    int e = 0;
+    CUDA_TRY(cudaMemcpyAsync(&e, err_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (e == SMIP_DEV_ERR_TIMEOUT)
+        return fail(SMIP_E_TIMEOUT, "a bounded device wait expired; results of the affected batch are incomplete");
+    if (e == SMIP_DEV_ERR_OUT_OF_RANGE)
+        return fail(SMIP_E_OUT_OF_RANGE, "Bispectrum: element address out of bounds (get_element would throw)");
+    return SMIP_OK;
+}
+
+} // namespace
+
+// ------------------------------------------------------------------- stack
+struct smip_stack {
+    int device = 0;
+    DeviceCtx* ctx = nullptr;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    Geometry g {};
+    long bdepth_req = 0;
+    int Bf = 0;                   // frames per batch
+    int fpc = 16;                 // frames per column-pass chunk
+    int dtype = -1;               // frame dtype fixed by the first push
+    int mode = 0;                 // 0 unset, 1 frames, 2 spectra
+    long nframes = 0;             // frames accumulated (incl. pending)
+    int pending = 0;              // frames staged for the next batch
+    bool has_ref = false;
+    // device buffers
+    float2 *B = nullptr, *C = nullptr, *Bn = nullptr;
+    double* P = nullptr;
+    double* Ppart = nullptr;
+    void* sum = nullptr;          // u64 (integer frames) or double
+    void* staging = nullptr;      // Bf raw frames
+    double* spec_staging = nullptr; // spectra input (mode 2)
+    void* ref = nullptr;          // raw frame 0
+    double* ref_sq = nullptr;
+    float2 *Gt = nullptr, *S = nullptr, *R = nullptr;
+    float* corr = nullptr;
+    int* shifts = nullptr;        // all frames, int2
+    long shifts_cap = 0;
+    int* err = nullptr;
+    Reco reco;
+    double2* Z = nullptr;
+    double* pfull = nullptr;
+    double* maxbuf = nullptr;
+
+    ~smip_stack()
+    {
+        cudaSetDevice(device);
+        if (st)
+            cudaStreamSynchronize(st);
+        dfree(B); dfree(C); dfree(Bn); dfree(P); dfree(Ppart);
+        if (sum) cudaFree(sum);
+        if (staging) cudaFree(staging);
+        dfree(spec_staging);
+        if (ref) cudaFree(ref);
+        dfree(ref_sq); dfree(Gt); dfree(S); dfree(R); dfree(corr); dfree(shifts); dfree(err);
+        dfree(Z); dfree(pfull); dfree(maxbuf);
+        if (own_stream && st)
+            cudaStreamDestroy(st);
+    }
+
+    size_t frame_elems() const { return (size_t)g.W * g.H; }
+    size_t half_elems() const { return (size_t)g.hw * g.H; }
+
+    int alloc()
+    {
+        const size_t bs = (size_t)g.base_size;
+        CUDA_TRY(cudaMalloc(&B, sizeof(float2) * bs));
+        CUDA_TRY(cudaMalloc(&C, sizeof(float2) * bs));
+        CUDA_TRY(cudaMemsetAsync(B, 0, sizeof(float2) * bs, st));
+        CUDA_TRY(cudaMemsetAsync(C, 0, sizeof(float2) * bs, st));
+        CUDA_TRY(cudaMalloc(&P, sizeof(double) * half_elems()));
+        CUDA_TRY(cudaMemsetAsync(P, 0, sizeof(double) * half_elems(), st));
+        const int nchunks = (Bf + fpc - 1) / fpc;
+        CUDA_TRY(cudaMalloc(&Ppart, sizeof(double) * half_elems() * nchunks));
+        CUDA_TRY(cudaMalloc(&sum, 8 * frame_elems()));
+        CUDA_TRY(cudaMemsetAsync(sum, 0, 8 * frame_elems(), st));
+        CUDA_TRY(cudaMalloc(&Gt, sizeof(float2) * half_elems() * Bf));
+        CUDA_TRY(cudaMalloc(&S, sizeof(float2) * half_elems() * Bf));
+        CUDA_TRY(cudaMalloc(&R, sizeof(float2) * half_elems()));
+        CUDA_TRY(cudaMalloc(&corr, sizeof(float) * frame_elems() * Bf));
+        CUDA_TRY(cudaMalloc(&ref_sq, sizeof(double)));
+        CUDA_TRY(cudaMalloc(&err, sizeof(int)));
+        CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
+        return SMIP_OK;
+    }
+
+    int ensure_shift_cap(long n)
+    {
+        if (n <= shifts_cap)
+            return SMIP_OK;
+        long cap = std::max<long>(n, std::max<long>(1024, 2 * shifts_cap));
+        int* nb = nullptr;
+        CUDA_TRY(cudaMalloc(&nb, sizeof(int) * 2 * cap));
+        if (shifts)
+            CUDA_TRY(cudaMemcpyAsync(nb, shifts, sizeof(int) * 2 * shifts_cap, cudaMemcpyDeviceToDevice, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        dfree(shifts);
+        shifts = nb;
+        shifts_cap = cap;
+        return SMIP_OK;
+    }
+
+    int run_batch()
+    {
+        const int n = pending;
+        if (n == 0)
+            return SMIP_OK;
+        const long first_index = nframes - n;
+        if (mode == 2) {
+            CUDA_TRY(launch_import_spectra(spec_staging, n, g, S, st));
+        } else {
+            const size_t fe = frame_elems();
+            const bool first = !has_ref;
+            int rc = ensure_shift_cap(nframes);
+            if (rc)
+                return rc;
+            if (first) {
+                CUDA_TRY(cudaMemcpyAsync(ref, staging, dtype_size(dtype) * fe, cudaMemcpyDeviceToDevice, st));
+                CUDA_TRY(launch_sumsq(dtype, ref, (long long)fe, ref_sq, st));
+            }
+            CUDA_TRY(launch_row_pass(dtype, staging, (long long)fe, n, g, Gt, ctx->tw32, st));
+            if (first)
+                CUDA_TRY(launch_col_pass(1, Gt, S, R, R, Ppart, 1, fpc, 0, g, ctx->tw32, st));
+            CUDA_TRY(launch_col_pass(0, Gt, S, R, nullptr, Ppart, n, fpc, first ? 1 : 0, g, ctx->tw32, st));
+            CUDA_TRY(launch_power_reduce(P, Ppart, (n + fpc - 1) / fpc, g, st));
+            CUDA_TRY(launch_xcorr_rows(Gt, corr, n, g, ctx->tw32, st));
+            CUDA_TRY(launch_xcorr_shift(dtype, corr, staging, (long long)fe, ref, ref_sq, n, first ? 1 : 0, g,
+                                        shifts + 2 * first_index, st));
+            CUDA_TRY(launch_saa_add(dtype, sum, staging, (long long)fe, n, first ? 1 : 0, shifts + 2 * first_index, g, st));
+            has_ref = true;
+        }
+        BispecLaunch L;
+        L.S = S;
+        L.nframes = n;
+        L.B = B;
+        L.C = C;
+        L.err = err;
+        L.num_sms = ctx->num_sms;
+        CUDA_TRY(launch_bispec_accumulate(L, g, st));
+        pending = 0;
+        return SMIP_OK;
+    }
+};
+
+static int check_stack(smip_stack_t s)
+{
+    if (!s)
+        return fail(SMIP_E_INVALID_ARGUMENT, "null stack handle");
+    if (cudaSetDevice(s->device) != cudaSuccess)
+        return fail(SMIP_E_CUDA, "cudaSetDevice failed");
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_create(smip_stack_t* out, int device, long ncols, long nrows, long bdepth, void* stream,
+                                 long batch_frames)
+{
+    if (!out)
+        return fail(SMIP_E_INVALID_ARGUMENT, "out is null");
+    *out = nullptr;
+    Geometry g;
+    int rc = make_geometry(ncols, nrows, bdepth, &g);
+    if (rc)
+        return rc;
+    DeviceCtx* ctx = nullptr;
+    rc = device_ctx(device, &ctx);
+    if (rc)
+        return rc;
+    smip_stack* s = new smip_stack();
+    s->device = device;
+    s->ctx = ctx;
+    s->g = g;
+    s->bdepth_req = bdepth;
+    if (batch_frames <= 0) {
+        const size_t per = sizeof(float2) * (size_t)g.hw * g.H;
+        long bf = (long)((64ull << 20) / per);
+        batch_frames = std::min<long>(256, std::max<long>(16, bf / 16 * 16));
+    }
+    s->Bf = (int)batch_frames;
+    if (stream) {
+        s->st = static_cast<cudaStream_t>(stream);
+    } else {
+        if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) {
+            delete s;
+            return fail(SMIP_E_CUDA, "cudaStreamCreate failed");
+        }
+        s->own_stream = true;
+    }
+    rc = s->alloc();
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_destroy(smip_stack_t s)
+{
+    if (!s)
+        return SMIP_OK;
+    delete s;
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_push_frames(smip_stack_t s, const void* frames, int dtype, long count, long stride_bytes,
+                                      int on_device)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    const size_t es = dtype_size(dtype);
+    if (!es)
+        return fail(SMIP_E_INVALID_ARGUMENT, "unknown frame dtype");
+    if (count < 0 || (count > 0 && !frames))
+        return fail(SMIP_E_INVALID_ARGUMENT, "invalid frame buffer");
+    if (s->mode == 2)
+        return fail(SMIP_E_INVALID_ARGUMENT, "stack accumulates spectra; frames cannot be mixed in");
+    if (s->dtype >= 0 && s->dtype != dtype)
+        return fail(SMIP_E_INVALID_ARGUMENT, "frame dtype differs from the stack's first frames");
+    const size_t fbytes = es * s->frame_elems();
+    if (stride_bytes == 0)
+        stride_bytes = (long)fbytes;
+    if ((size_t)stride_bytes < fbytes)
+        return fail(SMIP_E_INVALID_ARGUMENT, "frame stride smaller than a frame");
+    if (s->dtype < 0) {
+        s->dtype = dtype;
+        s->mode = 1;
+        CUDA_TRY(cudaMalloc(&s->staging, fbytes * s->Bf));
+        CUDA_TRY(cudaMalloc(&s->ref, fbytes));
+    }
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const char* src = static_cast<const char*>(frames);
+    long done = 0;
+    while (done < count) {
+        const long k = std::min<long>(count - done, s->Bf - s->pending);
+        char* dst = static_cast<char*>(s->staging) + fbytes * s->pending;
+        if ((size_t)stride_bytes == fbytes)
+            CUDA_TRY(cudaMemcpyAsync(dst, src + done * stride_bytes, fbytes * k, kind, s->st));
+        else
+            CUDA_TRY(cudaMemcpy2DAsync(dst, fbytes, src + done * stride_bytes, stride_bytes, fbytes, k, kind, s->st));
+        s->pending += (int)k;
+        s->nframes += k;
+        done += k;
+        if (s->pending == s->Bf) {
+            rc = s->run_batch();
+            if (rc)
+                return rc;
+        }
+    }
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_accumulate_fft(smip_stack_t s, const double* spectra, long count, int on_device)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    if (count < 0 || (count > 0 && !spectra))
+        return fail(SMIP_E_INVALID_ARGUMENT, "invalid spectrum buffer");
+    if (s->mode == 1)
+        return fail(SMIP_E_INVALID_ARGUMENT, "stack accumulates frames; spectra cannot be mixed in");
+    const size_t sbytes = sizeof(double) * 2 * s->frame_elems();
+    if (s->mode == 0) {
+        s->mode = 2;
+        CUDA_TRY(cudaMalloc(&s->spec_staging, sbytes * s->Bf));
+    }
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    long done = 0;
+    while (done < count) {
+        const long k = std::min<long>(count - done, s->Bf - s->pending);
+        CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char*>(s->spec_staging) + sbytes * s->pending,
+                                 reinterpret_cast<const char*>(spectra) + sbytes * done, sbytes * k, kind, s->st));
+        s->pending += (int)k;
+        s->nframes += k;
+        done += k;
+        if (s->pending == s->Bf) {
+            rc = s->run_batch();
+            if (rc)
+                return rc;
+        }
+    }
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_flush(smip_stack_t s)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    return s->run_batch();
+}
+
+extern "C" int smip_stack_sync(smip_stack_t s)
+{
+    int rc = smip_stack_flush(s);
+    if (rc)
+        return rc;
+    return check_dev_err(s->err, s->st);
+}
+
+extern "C" int smip_stack_frame_count(smip_stack_t s, long* n)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    if (n)
+        *n = s->nframes;
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_bispectrum_size(smip_stack_t s, long* n)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    if (n)
+        *n = (long)s->g.base_size;
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_shifts(smip_stack_t s, int* xy, long first, long count)
+{
+    int rc = smip_stack_sync(s);
+    if (rc)
+        return rc;
+    if (s->mode != 1)
+        return fail(SMIP_E_BAD_CALL, "no frames have been correlated");
+    if (first < 0 || count < 0 || first + count > s->nframes)
+        return fail(SMIP_E_OUT_OF_RANGE, "frame range outside the stack");
+    CUDA_TRY(cudaMemcpyAsync(xy, s->shifts + 2 * first, sizeof(int) * 2 * count, cudaMemcpyDeviceToHost, s->st));
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    return SMIP_OK;
+}
+
+static int need_frames(smip_stack_t s)
+{
+    if (s->nframes == 0)
+        return fail(SMIP_E_RUNTIME, "division by zero: no frames accumulated");
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_sum(smip_stack_t s, double* out)
+{
+    int rc = smip_stack_sync(s);
+    if (rc || (rc = need_frames(s)))
+        return rc;
+    if (s->mode != 1)
+        return fail(SMIP_E_BAD_CALL, "no frames have been added to the sum");
+    const size_t n = s->frame_elems();
+    std::vector<uint64_t> raw(n);
+    CUDA_TRY(cudaMemcpyAsync(raw.data(), s->sum, 8 * n, cudaMemcpyDeviceToHost, s->st));
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    const double nf = (double)s->nframes;
+    if (s->dtype == SMIP_U8 || s->dtype == SMIP_U16) {
+        for (size_t i = 0; i < n; ++i)
+            out[i] = (double)raw[i] / nf; // exact integer sum, as the reference's double sum
+    } else {
+        for (size_t i = 0; i < n; ++i) {
+            double v;
+            std::memcpy(&v, &raw[i], 8);
+            out[i] = v / nf;
+        }
+    }
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_power(smip_stack_t s, double* out)
+{
+    int rc = smip_stack_sync(s);
+    if (rc || (rc = need_frames(s)))
+        return rc;
+    if (!s->pfull)
+        CUDA_TRY(cudaMalloc(&s->pfull, sizeof(double) * s->frame_elems()));
+    const double pnorm = (double)((size_t)s->nframes * s->frame_elems());
+    CUDA_TRY(launch_power_full(s->P, pnorm, s->g, s->pfull, s->st));
+    CUDA_TRY(cudaMemcpyAsync(out, s->pfull, sizeof(double) * s->frame_elems(), cudaMemcpyDeviceToHost, s->st));
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    return SMIP_OK;
+}
+
+static int normalize_bispec(smip_stack_t s)
+{
+    if (!s->Bn)
+        CUDA_TRY(cudaMalloc(&s->Bn, sizeof(float2) * s->g.base_size));
+    CUDA_TRY(launch_bispec_normalize(s->B, s->C, (double)s->nframes, s->g.base_size, s->Bn, s->st));
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_bispectrum(smip_stack_t s, float* out)
+{
+    int rc = smip_stack_sync(s);
+    if (rc || (rc = need_frames(s)))
+        return rc;
+    if ((rc = normalize_bispec(s)))
+        return rc;
+    CUDA_TRY(cudaMemcpyAsync(out, s->Bn, sizeof(float2) * s->g.base_size, cudaMemcpyDeviceToHost, s->st));
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    return SMIP_OK;
+}
+
+static int stack_reco(smip_stack_t s, double R)
+{
+    int rc = smip_stack_sync(s);
+    if (rc || (rc = need_frames(s)))
+        return rc;
+    if (!(R >= 0.0))
+        return fail(SMIP_E_INVALID_ARGUMENT, "reco_radius must be >= 0");
+    if ((rc = normalize_bispec(s)))
+        return rc;
+    s->reco.g = s->g;
+    return s->reco.run(s->Bn, R, s->err, s->st);
+}
+
+extern "C" int smip_stack_reconstruct(smip_stack_t s, double R, double* phases, unsigned char* flags, double* cons)
+{
+    int rc = stack_reco(s, R);
+    if (rc)
+        return rc;
+    if ((rc = s->reco.download(phases, flags, cons, s->st)))
+        return rc;
+    return check_dev_err(s->err, s->st);
+}
+
+extern "C" int smip_stack_finish(smip_stack_t s, double R, double* image, double* phases, unsigned char* flags,
+                                 double* cons)
+{
+    int rc = stack_reco(s, R);
+    if (rc)
+        return rc;
+    if (s->mode != 1)
+        return fail(SMIP_E_BAD_CALL, "the final image needs the power spectrum of pushed frames");
+    if (!(R > 0.0))
+        return fail(SMIP_E_DOMAIN, "WindowFunction aperture size <= 0");
+    const size_t n = s->frame_elems();
+    if (!s->Z) {
+        CUDA_TRY(cudaMalloc(&s->Z, sizeof(double2) * n));
+        CUDA_TRY(cudaMalloc(&s->maxbuf, sizeof(double)));
+    }
+    const double pnorm = (double)((size_t)s->nframes * n);
+    CUDA_TRY(launch_finish(s->P, pnorm, s->reco.phases, 2.0 * R, s->g, s->Z, nullptr, s->maxbuf, s->ctx->tw64, s->st));
+    if (image)
+        CUDA_TRY(cudaMemcpyAsync(image, s->Z, sizeof(double2) * n, cudaMemcpyDeviceToHost, s->st));
+    if ((rc = s->reco.download(phases, flags, cons, s->st)))
+        return rc;
+    return check_dev_err(s->err, s->st);
+}
+
+extern "C" int smip_stack_share_reference(smip_stack_t dst, smip_stack_t src)
+{
+    int rc = smip_stack_sync(dst);
+    if (rc)
+        return rc;
+    if (!src || src->device != dst->device)
+        return fail(SMIP_E_INVALID_ARGUMENT, "stacks must live on the same device");
+    if (!dst->has_ref)
+        return fail(SMIP_E_BAD_CALL, "dst has no reference frame yet");
+    if (src->g.W != dst->g.W || src->g.H != dst->g.H || src->g.De != dst->g.De)
+        return fail(SMIP_E_INVALID_ARGUMENT, "Bispectrum::operator+=(const Bispectrum) : operand dimension size mismatch");
+    if (src->nframes != 0)
+        return fail(SMIP_E_BAD_CALL, "src already holds frames");
+    const size_t fbytes = dtype_size(dst->dtype) * dst->frame_elems();
+    src->dtype = dst->dtype;
+    src->mode = 1;
+    CUDA_TRY(cudaMalloc(&src->staging, fbytes * src->Bf));
+    CUDA_TRY(cudaMalloc(&src->ref, fbytes));
+    CUDA_TRY(cudaMemcpy(src->ref, dst->ref, fbytes, cudaMemcpyDeviceToDevice));
+    CUDA_TRY(cudaMemcpy(src->R, dst->R, sizeof(float2) * dst->half_elems(), cudaMemcpyDeviceToDevice));
+    CUDA_TRY(cudaMemcpy(src->ref_sq, dst->ref_sq, sizeof(double), cudaMemcpyDeviceToDevice));
+    src->has_ref = true;
+    return SMIP_OK;
+}
+
+__global__ void add_u64_kernel(unsigned long long* d, const unsigned long long* s, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] += s[i];
+}
+__global__ void add_f64_kernel(double* d, const double* s, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] += s[i];
+}
+
+extern "C" int smip_stack_merge(smip_stack_t dst, smip_stack_t src)
+{
+    int rc = smip_stack_sync(dst);
+    if (rc || (rc = smip_stack_sync(src)))
+        return rc;
+    if (src->device != dst->device)
+        return fail(SMIP_E_INVALID_ARGUMENT, "stacks must live on the same device");
+    if (src->g.W != dst->g.W || src->g.H != dst->g.H || src->g.De != dst->g.De)
+        return fail(SMIP_E_INVALID_ARGUMENT, "Bispectrum::operator+=(const Bispectrum) : operand dimension size mismatch");
+    if (src->mode != dst->mode || (src->mode == 1 && src->dtype != dst->dtype))
+        return fail(SMIP_E_INVALID_ARGUMENT, "stacks accumulate different inputs");
+    CUDA_TRY(launch_bispec_merge(dst->B, dst->C, src->B, src->C, dst->g.base_size, dst->st));
+    add_f64_kernel<<<256, 256, 0, dst->st>>>(dst->P, src->P, (long long)dst->half_elems());
+    if (dst->mode == 1) {
+        if (dst->dtype == SMIP_U8 || dst->dtype == SMIP_U16)
+            add_u64_kernel<<<256, 256, 0, dst->st>>>((unsigned long long*)dst->sum, (const unsigned long long*)src->sum,
+                                                     (long long)dst->frame_elems());
+        else
+            add_f64_kernel<<<256, 256, 0, dst->st>>>((double*)dst->sum, (const double*)src->sum,
+                                                     (long long)dst->frame_elems());
+        rc = dst->ensure_shift_cap(dst->nframes + src->nframes);
+        if (rc)
+            return rc;
+        CUDA_TRY(cudaMemcpyAsync(dst->shifts + 2 * dst->nframes, src->shifts, sizeof(int) * 2 * src->nframes,
+                                 cudaMemcpyDeviceToDevice, dst->st));
+    }
+    dst->nframes += src->nframes;
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(dst->st));
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_save_bispectrum(smip_stack_t s, const char* path)
+{
+    if (!path)
+        return fail(SMIP_E_INVALID_ARGUMENT, "null path");
+    long n = 0;
+    int rc = smip_stack_bispectrum_size(s, &n);
+    if (rc)
+        return rc;
+    std::vector<float> buf(2 * (size_t)n);
+    if ((rc = smip_stack_bispectrum(s, buf.data())))
+        return rc;
+    FILE* f = std::fopen(path, "wb");
+    if (!f)
+        return fail(SMIP_E_RUNTIME, std::string("unable to open file ") + path + " for writing");
+    // bispectrum.h:421-428: size_t base_size, 4 x size_t dims, T[base_size]
+    const size_t hdr[5] = { (size_t)n, (size_t)s->g.W, (size_t)s->g.H, (size_t)s->bdepth_req, (size_t)s->bdepth_req };
+    bool ok = std::fwrite(hdr, sizeof(size_t), 5, f) == 5;
+    ok = ok && std::fwrite(buf.data(), sizeof(float) * 2, (size_t)n, f) == (size_t)n;
+    std::fclose(f);
+    if (!ok)
+        return fail(SMIP_E_RUNTIME, std::string("error writing ") + path);
+    return SMIP_OK;
+}
+
+// ------------------------------------------------------- standalone calls
+extern "C" int smip_next_reco_index(double* r, double* phi, int* i, int* j)
+{
+    if (!r || !phi || !i || !j)
+        return fail(SMIP_E_INVALID_ARGUMENT, "null argument");
+    next_reco_index(*r, *phi, *i, *j);
+    return SMIP_OK;
+}
+
+extern "C" int smip_reco_visits(double R, int* ij, long cap, long* count)
+{
+    std::vector<int2> v = reco_visits(R);
+    if (count)
+        *count = (long)v.size();
+    if (ij)
+        for (long q = 0; q < (long)v.size() && q < cap; ++q) {
+            ij[2 * q] = v[q].x;
+            ij[2 * q + 1] = v[q].y;
+        }
+    return SMIP_OK;
+}
+
+extern "C" int smip_reconstruct_phases(int device, const float* bispec, long xsize, long ysize, long bdepth, double R,
+                                       double* phases, unsigned char* flags, double* cons)
+{
+    Geometry g;
+    int rc = make_geometry(xsize, ysize, bdepth, &g);
+    if (rc)
+        return rc;
+    if (!bispec)
+        return fail(SMIP_E_INVALID_ARGUMENT, "null bispectrum");
+    DeviceCtx* ctx = nullptr;
+    if ((rc = device_ctx(device, &ctx)))
+        return rc;
+    CUDA_TRY(cudaSetDevice(device));
+    cudaStream_t st;
+    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    float2* Bd = nullptr;
+    int* err = nullptr;
+    rc = SMIP_OK;
+    {
+        Reco reco;
+        reco.g = g;
+        if (cudaMalloc(&Bd, sizeof(float2) * g.base_size) != cudaSuccess || cudaMalloc(&err, sizeof(int)) != cudaSuccess)
+            rc = fail(SMIP_E_NO_MEMORY, "device allocation failed");
+        if (!rc && cudaMemcpyAsync(Bd, bispec, sizeof(float2) * g.base_size, cudaMemcpyHostToDevice, st) != cudaSuccess)
+            rc = fail(SMIP_E_CUDA, "bispectrum upload failed");
+        if (!rc && cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess)
+            rc = fail(SMIP_E_CUDA, "memset failed");
+        if (!rc)
+            rc = reco.run(Bd, R, err, st);
+        if (!rc)
+            rc = reco.download(phases, flags, cons, st);
+        if (!rc)
+            rc = check_dev_err(err, st);
+        cudaStreamSynchronize(st);
+    }
+    if (Bd) cudaFree(Bd);
+    if (err) cudaFree(err);
+    cudaStreamDestroy(st);
+    return rc;
+}
+
+extern "C" int smip_xcorr_displacement(int device, const double* refimg, const double* frame, long ncols, long nrows,
+                                       int* dx, int* dy, double* corr_out)
+{
+    if (!refimg || !frame || !dx || !dy)
+        return fail(SMIP_E_INVALID_ARGUMENT, "null argument");
+    smip_stack_t s = nullptr;
+    int rc = smip_stack_create(&s, device, ncols, nrows, 8, nullptr, 16);
+    if (rc)
+        return rc;
+    const size_t n = (size_t)ncols * nrows;
+    std::vector<double> two(2 * n);
+    std::memcpy(two.data(), refimg, sizeof(double) * n);
+    std::memcpy(two.data() + n, frame, sizeof(double) * n);
+    rc = smip_stack_push_frames(s, two.data(), SMIP_F64, 2, 0, 0);
+    if (!rc)
+        rc = smip_stack_sync(s);
+    if (!rc) {
+        int xy[2];
+        rc = smip_stack_shifts(s, xy, 1, 1);
+        *dx = xy[0];
+        *dy = xy[1];
+        if (!rc && corr_out) {
+            // corr of frame 1 of the batch, FP32 -> double
+            std::vector<float> c(n);
+            if (cudaMemcpy(c.data(), s->corr + n, sizeof(float) * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+                rc = fail(SMIP_E_CUDA, "correlation download failed");
+            for (size_t i = 0; i < n && !rc; ++i)
+                corr_out[i] = c[i];
+        }
+    }
+    smip_stack_destroy(s);
+    return rc;
+}
+
+extern "C" int smip_hann(int device, double* out, long xsize, long ysize, double aperture)
+{
+    if (!out)
+        return fail(SMIP_E_INVALID_ARGUMENT, "null output");
+    if (!(aperture > 0.))
+        return fail(SMIP_E_DOMAIN, "WindowFunction aperture size <= 0");
+    if (!pow2(xsize) || !pow2(ysize))
+        return fail(SMIP_E_UNSUPPORTED, "window size must be a power of two per axis");
+    CUDA_TRY(cudaSetDevice(device));
+    double* d = nullptr;
+    CUDA_TRY(cudaMalloc(&d, sizeof(double) * xsize * ysize));
+    cudaError_t e = launch_hann(d, (int)xsize, (int)ysize, aperture, 0);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(out, d, sizeof(double) * xsize * ysize, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess)
+        return fail(SMIP_E_CUDA, cudaGetErrorString(e));
+    return SMIP_OK;
+}

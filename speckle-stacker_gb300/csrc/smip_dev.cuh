@@ -1,0 +1,201 @@
+// smip_dev.cuh -- device helpers shared by the SMIP kernels (sm_103a).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "smip_internal.h"
+
+namespace smip_gpu {
+
+// ---------------------------------------------------------------- complex ops
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+template <typename C> struct real_of;
+template <> struct real_of<float2> { using type = float; };
+template <> struct real_of<double2> { using type = double; };
+
+__device__ __forceinline__ unsigned bitrev(unsigned i, int logn) { return __brev(i) >> (32 - logn); }
+
+// In-place radix-2 decimation-in-time FFT of nl lines of length n = 1<<logn
+// held in shared memory (line stride ls), input already in bit-reversed order.
+// tw[k] = exp(-2*pi*i*k / 2^twlog) for k < 2^(twlog-1); sign -1 forward, +1
+// inverse (unnormalised).  Called by all threads of the block.
+template <typename C>
+__device__ void fft_stages(C* buf, int logn, int nl, int ls, const C* tw, int twlog, int sign)
+{
+    const int n = 1 << logn;
+    const int nb = nl * (n >> 1);
+    for (int s = 1; s <= logn; ++s) {
+        const int half = 1 << (s - 1);
+        const int tsh = twlog - s;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+            const int line = b >> (logn - 1);
+            const int q = b & ((n >> 1) - 1);
+            const int k = q & (half - 1);
+            const int i0 = ((q >> (s - 1)) << s) + k;
+            C w = tw[k << tsh];
+            if (sign > 0)
+                w.y = -w.y;
+            C* L = buf + line * ls;
+            const C a = L[i0];
+            const C t = cmul(L[i0 + half], w);
+            L[i0] = cadd(a, t);
+            L[i0 + half] = csub(a, t);
+        }
+        __syncthreads();
+    }
+}
+
+// Copies the twiddle table (2^(twlog-1) entries) into shared memory.
+template <typename C>
+__device__ void load_twiddles(C* dst, const C* src, int twlog)
+{
+    for (int k = threadIdx.x; k < (1 << (twlog - 1)); k += blockDim.x)
+        dst[k] = src[k];
+}
+
+// --------------------------------------------------- bispectrum element index
+// Device replica of Bispectrum<T>::get_element's index path
+// (include/bispectrum.h:482-512 with canonicalize_indices 553-589,
+// classify_indices 162-174 and calc_offset 324-349), including the silent
+// modulo-2^64 wrap of calc_offset.  Returns the packed offset or -1 where the
+// reference throws std::out_of_range.  d: 4 sizes, 4 base sizes, min, max.
+struct BispecDims {
+    int sizes[4];
+    int base[4];
+    int mn[4];
+    int mx[4];
+    long long base_size;
+};
+
+__device__ __forceinline__ long long bispec_get_offset(const BispecDims& d, int i0, int i1, int i2, int i3, int* conj)
+{
+    if (abs(i2) > d.mx[2] || abs(i3) > d.mx[3]) {
+        int t = i0; i0 = i2; i2 = t;
+        t = i1; i1 = i3; i3 = t;
+    }
+    if (i0 < d.mn[0] || i0 > d.mx[0] || i1 < d.mn[1] || i1 > d.mx[1] || i2 < d.mn[2] || i2 > d.mx[2]
+        || i3 < d.mn[3] || i3 > d.mx[3])
+        return -1;
+    int u0, u1, u2, u3, cj = 0;
+    if (i0 <= 0 && i2 <= 0) { u0 = i0; u1 = i1; u2 = i2; u3 = i3; }
+    else if (i0 > 0 && i2 > 0) { cj = 1; u0 = -i0; u1 = -i1; u2 = -i2; u3 = -i3; }
+    else if (i0 > 0) {
+        if (i0 + i2 > 0) { u0 = -i0 - i2; u1 = -i1 - i3; u2 = i2; u3 = i3; }
+        else { cj = 1; u0 = -i0; u1 = -i1; u2 = i2 + i0; u3 = i3 + i1; }
+    } else {
+        if (i0 + i2 > 0) { u0 = i0; u1 = i1; u2 = -i2 - i0; u3 = -i3 - i1; }
+        else { cj = 1; u0 = i0 + i2; u1 = i1 + i3; u2 = -i2; u3 = -i3; }
+    }
+    if (abs(u2) > d.mx[2] || abs(u3) > d.mx[3]) {
+        int t = u0; u0 = u2; u2 = t;
+        t = u1; u1 = u3; u3 = t;
+    }
+    int a0 = -u0, a1 = u1, a2 = -u2, a3 = u3;
+    if (a0 < 0) a0 += d.sizes[0];
+    if (a1 < 0) a1 += d.sizes[1];
+    if (a2 < 0) a2 += d.sizes[2];
+    if (a3 < 0) a3 += d.sizes[3];
+    unsigned long long addr = (unsigned long long)(long long)a0;
+    addr = addr * (unsigned long long)d.base[1] + (unsigned long long)(long long)a1;
+    addr = addr * (unsigned long long)d.base[2] + (unsigned long long)(long long)a2;
+    addr = addr * (unsigned long long)d.base[3] + (unsigned long long)(long long)a3;
+    if (addr >= (unsigned long long)d.base_size)
+        return -1;
+    *conj = cj;
+    return (long long)addr;
+}
+
+// ------------------------------------------------------ bounded device waits
+// Every spin in these kernels is bounded by wall time (%globaltimer); on
+// expiry the waiting thread records SMIP_DEV_ERR_TIMEOUT and gives up.
+__device__ __forceinline__ uint64_t globaltimer_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void record_error(int* err, int code)
+{
+    if (err)
+        atomicCAS(err, 0, code);
+}
+
+// --------------------------------------------------------- mbarrier and TMA
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+// Waits for the barrier phase with the given parity; false after timeout_ns.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t timeout_ns)
+{
+    if (mbar_try_wait(bar, parity))
+        return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (;;) {
+        for (int i = 0; i < 64; ++i)
+            if (mbar_try_wait(bar, parity))
+                return true;
+        if (globaltimer_ns() - t0 > timeout_ns)
+            return false;
+    }
+}
+
+// 3-D tiled TMA load into shared memory, completion signalled on bar.
+__device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, int x, int y, int z, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(tmap), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+} // namespace smip_gpu

@@ -1,0 +1,109 @@
+// smip_internal.h -- declarations shared by the SMIP host runtime and kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace smip_gpu {
+
+// device-side error codes written to a stack's error word
+enum : int {
+    SMIP_DEV_OK = 0,
+    SMIP_DEV_ERR_TIMEOUT = 1,      // a bounded mbarrier wait expired
+    SMIP_DEV_ERR_OUT_OF_RANGE = 2, // Bispectrum::get_element would throw
+};
+
+constexpr int kMaxLog = 9;        // frames up to 512 x 512
+constexpr int kTwLog = kMaxLog;   // twiddle table for length 2^kTwLog
+constexpr int kRowBlock = 16;     // rows per CTA in the row passes
+constexpr int kColLines = 4;      // frames per FFT pass in the column kernel
+
+// Geometry of one stack (all derived from ncols = W, nrows = H, depth).
+struct Geometry {
+    int W, H;         // frame size (powers of two)
+    int logW, logH;
+    int hw;           // W/2 + 1: u_x half-plane rows a = -x in [0, W/2]
+    int De;           // bispectrum depth rounded down to even
+    int E;            // packed elements per (u_x, u_y): (De/2+1)(De+1)
+    long long base_size;
+};
+
+// ---------------------------------------------------------------- launchers
+// All launchers are asynchronous on `st` and return cudaGetLastError().
+
+// frames (dtype) -> G'(a, y) = sum_x f(x,y) exp(+2 pi i a x / W), stored
+// [f][a][y] (float2).  dtype: 0 u8, 1 u16, 2 f32, 3 f64.
+cudaError_t launch_row_pass(int dtype, const void* frames, long long frame_stride_elems, int nframes,
+                            const Geometry& g, float2* Gt, const float2* tw, cudaStream_t st);
+
+// Column pass.  mode 1: frame 0 only -> Rbuf (the reference spectrum).
+// mode 0: S[f][a][c] = F(-a, c - H/2), power partials, and the inverse column
+// FFT of conj(R)·F for the cross correlation written back into Gt.
+cudaError_t launch_col_pass(int mode, float2* Gt, float2* S, const float2* Rbuf, float2* Rout, double* Ppart,
+                            int nframes, int frames_per_chunk, int skip_xcorr_frame0, const Geometry& g,
+                            const float2* tw, cudaStream_t st);
+cudaError_t launch_power_reduce(double* P, const double* Ppart, int nchunks, const Geometry& g, cudaStream_t st);
+
+// Row pass of the correlation's inverse transform: corr[f][y][x] (float).
+cudaError_t launch_xcorr_rows(const float2* Gt, float* corr, int nframes, const Geometry& g, const float2* tw,
+                              cudaStream_t st);
+
+// Integer shift per frame: FP32 correlation peak, candidates re-scored exactly.
+// ref_sq: sum of squares of the reference frame (double, device).
+cudaError_t launch_xcorr_shift(int dtype, const float* corr, const void* frames, long long frame_stride_elems,
+                               const void* ref, const double* ref_sq, int nframes, int first_is_frame0,
+                               const Geometry& g, int* shifts, cudaStream_t st);
+
+// sum += |frames| shifted back by their shifts (Array2::shifted semantics);
+// the stack's frame 0 enters with its sign (smip-cli/main.cpp:266).
+cudaError_t launch_saa_add(int dtype, void* sum, const void* frames, long long frame_stride_elems, int nframes,
+                           int first_is_frame0, const int* shifts, const Geometry& g, cudaStream_t st);
+
+// FFT-order complex<double> spectra -> S layout (float2).
+cudaError_t launch_import_spectra(const double* spectra, int nframes, const Geometry& g, float2* S, cudaStream_t st);
+
+// Bispectrum accumulation over a batch of spectra S[0..nframes).
+struct BispecLaunch {
+    const float2* S;     // [nframes][hw][H]
+    int nframes;
+    float2* B;           // packed bispectrum
+    float2* C;           // Kahan compensation, same layout
+    int* err;
+    int num_sms;
+};
+cudaError_t launch_bispec_accumulate(const BispecLaunch& L, const Geometry& g, cudaStream_t st);
+bool bispec_depth_supported(int De);
+
+// out = (B - C) / nframes  (float2 packed), or plain add dst += src for merge.
+cudaError_t launch_bispec_normalize(const float2* B, const float2* C, double nframes, long long n, float2* out,
+                                    cudaStream_t st);
+cudaError_t launch_bispec_merge(float2* Bd, float2* Cd, const float2* Bs, const float2* Cs, long long n,
+                                cudaStream_t st);
+
+// Closure-phase recovery (one CTA per job).
+struct RecoJob {
+    const float2* B;     // normalised packed bispectrum
+    const int2* visits;  // spiral visit list
+    int nvisits;
+    int W, H, De;
+    double2* phases;     // W*H, FFT order
+    float2* phf;         // FP32 mirror of phases (scratch)
+    double* cons;        // W*H
+    unsigned char* flags;
+    int* err;
+};
+cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int max_H, cudaStream_t st);
+
+// Final image (double precision): Z = sqrt(P_norm) * (phases * hann), inverse
+// FFT, divide by max |.|.  Also writes the full-plane normalised power.
+cudaError_t launch_finish(const double* Phalf, double pnorm, const double2* phases, double aperture,
+                          const Geometry& g, double2* Z, double* power_full, double* maxbuf, const double2* tw64,
+                          cudaStream_t st);
+cudaError_t launch_power_full(const double* Phalf, double pnorm, const Geometry& g, double* power_full,
+                              cudaStream_t st);
+cudaError_t launch_hann(double* out, int W, int H, double aperture, cudaStream_t st);
+
+// Sum of squares of a frame (double), for the correlation error bound.
+cudaError_t launch_sumsq(int dtype, const void* frame, long long n, double* out, cudaStream_t st);
+
+} // namespace smip_gpu
