@@ -1,0 +1,364 @@
+#!/usr/bin/env python3
+"""Benchmark of the SMIP per-frame pipeline on GB300.
+
+Workload: one speckle stack of 2000 frames of 256x256 uint16 (extended object,
+Kolmogorov PSFs at D/r0 = 15, Poisson + read noise), bispectrum depth 32,
+phase-reconstruction radius 128 -- smip-cli -b 32 -p 128 on that stack.
+
+A step = the per-frame pipeline over the whole stack: ingest, FFT, power
+spectrum, cross-correlation shift-and-add and bispectrum accumulation
+(smip-cli/main.cpp:246-312).  Metric: frames/s.  The phase reconstruction and
+final image (main.cpp:318-376) are timed separately as the reconstruction
+latency (p50/p99).
+
+  value  -- frames resident in HBM (262 MB, larger than L2) when timing starts
+  e2e    -- frames pushed from page-locked host memory through the C ABI
+            (host->device copies in the timed region), shifts read back
+  --impl reference -- the CPU oracle (plain-C port of the reference's hot
+            path) on the host cores, all threads, a bounded sample per step.
+
+Multi-GPU (torchrun): every rank processes its own stack (replicas, no
+collective on the data path); value = all frames / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "speckle-stacker_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "frames/s (bispectrum+SAA)"
+WORKLOAD = "extended256"
+
+
+def triples(n, d):
+    """Exact in-range triple count of bispectrum.h:393-408 for an n x n frame."""
+    d = (d // 2) * 2
+    tot = 0
+    for k in range(-d // 2, 1):
+        for i in range(-n // 2, 1):
+            if i + k < -n // 2:
+                continue
+            for l in range(-d // 2, d // 2 + 1):
+                tot += n - abs(l)
+    return tot
+
+
+def gen_frames(spec, nframes, procs):
+    """Frames [0, nframes) of the seeded stack, generated in a spawn pool."""
+    from smip_gb300 import synthetic as S
+
+    if procs <= 1:
+        return S.make_stack(spec, 0, nframes)
+    import multiprocessing as mp
+
+    chunk = (nframes + procs - 1) // procs
+    jobs = [(spec, s, min(chunk, nframes - s)) for s in range(0, nframes, chunk)]
+    with mp.get_context("spawn").Pool(procs) as pool:
+        parts = pool.starmap(S.make_stack, jobs)
+    return np.concatenate(parts)
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for name, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        finally:
+            os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def fp32_peak_tflops(torch, dev):
+    """FP32 CUDA-core peak measured with cuBLAS SGEMM (TF32 off), best of 5."""
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device=dev)
+    b = torch.randn(n, n, device=dev)
+    for _ in range(2):
+        a @ b
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def cpu_baseline(frames, depth, budget_s=12.0, threads=None):
+    """The CPU oracle (plain-C port of the reference's per-frame path) on the
+    host cores: frames/s over a bounded sample of the same stack."""
+    from oracle import Oracle, bispec_desc
+
+    O = Oracle()
+    threads = threads or os.cpu_count() or 1
+    n = frames.shape[1]
+    d = bispec_desc(n, n, depth)
+    B = np.zeros(d["base_size"], np.complex64)
+    P = np.zeros(n * n)
+    Ssum = np.zeros(n * n)
+    ref = frames[0].astype(np.float64)
+    done, t0 = 0, time.perf_counter()
+    while done < len(frames) and (time.perf_counter() - t0 < budget_s or done < 2):
+        O.accumulate_frames(frames[done:done + 1], depth, ref, B, P, Ssum, nthreads=threads)
+        done += 1
+    el = time.perf_counter() - t0
+    return {"value": done / el, "unit": "frames/s", "cores": threads, "kind": "port",
+            "sample": f"{done} frames of the {n}x{n} u16 stack (FFT, shift-and-add, power, bispectrum d={depth}), "
+                      f"{el:.1f} s"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from smip_gb300 import synthetic as S
+
+    spec = S.config_spec(WORKLOAD)
+    per_step = 4
+    frames = S.make_stack(spec, 0, per_step * (args.steps + args.warmup))
+    threads = os.cpu_count() or 1
+    from oracle import Oracle, bispec_desc
+
+    O = Oracle()
+    d = bispec_desc(spec.n, spec.n, spec.bdepth)
+    B = np.zeros(d["base_size"], np.complex64)
+    P = np.zeros(spec.n ** 2)
+    Ssum = np.zeros(spec.n ** 2)
+    ref = frames[0].astype(np.float64)
+    times = []
+    for s in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        O.accumulate_frames(frames[s * per_step:(s + 1) * per_step], spec.bdepth, ref, B, P, Ssum, nthreads=threads)
+        if s >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = per_step * args.steps / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded speckle frames)",
+        "config": {"workload": f"{WORKLOAD}: 2000 x 256x256 u16, bdepth 32, reco radius 128",
+                   "per_step_sample": f"{per_step} frames"},
+        "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
+                         "sample": f"{per_step} frames per step of the 256x256 u16 stack; plain-C port of "
+                                   "the reference's per-frame path (oracle/smip_oracle.c)"},
+        "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from smip_gb300 import synthetic as S
+    from smip_gb300.distributed import replica_seed
+
+    spec = S.config_spec(WORKLOAD, nframes=args.nframes, seed=replica_seed(2000, rank))
+    # frames first (spawn pool before any CUDA call)
+    t_gen = time.perf_counter()
+    frames = gen_frames(spec, args.nframes, min(16, os.cpu_count() or 1))
+    t_gen = time.perf_counter() - t_gen
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    import smip_gb300 as G
+
+    n, D, R = spec.n, spec.bdepth, float(spec.reco_radius)
+    nf = args.nframes
+    frames_dev = torch.from_numpy(frames.view(np.int16)).to(dev).view(torch.uint16)
+    pinned = torch.from_numpy(frames.view(np.int16)).pin_memory()
+    pinned_np = pinned.numpy().view(np.uint16)
+    stream = torch.cuda.Stream(device=dev)
+    st = G.Stack(n, n, D, device=local, stream=stream.cuda_stream)
+
+    def step_dev():
+        st.reset()
+        st.push_frames(frames_dev)
+        st.flush()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    for _ in range(args.warmup):
+        step_dev()
+    st.kernel_time()  # discard warm-up timing
+    st.set_timing(True)
+    launches0 = G.kernel_launches()
+    barrier()
+    with ClockSampler(local) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step_dev()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    launches = G.kernel_launches() - launches0
+    elapsed = max_over_ranks(e0.elapsed_time(e1) * 1e-3)
+    k2_ms, k2_n, k2_frames = st.kernel_time()
+    st.set_timing(False)
+    clocks = clk.summary()
+    value = world * nf * args.steps / elapsed
+
+    # end to end through the C ABI: page-locked host frames, H2D in the timed region
+    for _ in range(2):
+        st.reset()
+        st.push_frames(pinned_np)
+        st.shifts()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        st.reset()
+        st.push_frames(pinned_np)
+        sh = st.shifts()  # D2H of the step result (syncs)
+    torch.cuda.synchronize(dev)
+    e2e_el = max_over_ranks(time.perf_counter() - t0)
+    e2e = {"value": world * nf * args.steps / e2e_el, "unit": "frames/s",
+           "h2d_bytes_per_step": int(frames.nbytes), "d2h_bytes_per_step": int(sh.nbytes)}
+
+    # reconstruction latency (phase recovery + image) on the accumulated stack
+    rec = []
+    for _ in range(max(5, args.steps)):
+        t0 = time.perf_counter()
+        st.finish(R)
+        rec.append((time.perf_counter() - t0) * 1e3)
+    recon = {"p50_ms": float(np.percentile(rec, 50)), "p99_ms": float(np.percentile(rec, 99))}
+
+    # roofline of the dominant kernel (bispectrum accumulation, FP32-pipe bound)
+    T = triples(n, D)
+    peak = fp32_peak_tflops(torch, dev)
+    flops_per_launch = 14.0 * T * (k2_frames / max(k2_n, 1))
+    achieved = flops_per_launch / (k2_ms / max(k2_n, 1) * 1e-3) / 1e12 if k2_ms > 0 else None
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "bispec_accum_extended256.txt")
+    if os.path.exists(prof):
+        for line in open(prof):
+            if line.startswith("dram_bytes_per_launch_full_batch:"):
+                traffic = float(line.split(":")[1])
+    roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "kernel": "bispec_accum_kernel<32>", "launches": k2_n,
+                "avg_launch_ms": k2_ms / max(k2_n, 1), "frames_per_launch": k2_frames / max(k2_n, 1),
+                "algorithmic": f"14 FLOP x {T} triples per frame",
+                "peak_source": "cuBLAS FP32 SGEMM 8192^3, TF32 off, measured in this run"}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(frames[:64], D)
+    line = {
+        "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 phase recursion)",
+        "data": "synthetic (seeded speckle frames, Kolmogorov PSFs)",
+        "config": {"workload": f"{WORKLOAD}: {nf} x 256x256 u16 extended object, D/r0=15, bdepth 32, reco radius 128",
+                   "frames_per_step_per_gpu": nf, "l2": "inputs larger than L2 (262 MB frames per step)",
+                   "parallelism": f"replicas x{world}", "batch_frames": None},
+        "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
+        "clocks": clocks, "recon_latency": recon,
+        "bispec_kernel_frames_per_s": (k2_frames / (k2_ms * 1e-3)) if k2_ms > 0 else None,
+        "frame_generation_s": t_gen,
+    }
+    st.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nframes", type=int, default=2000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

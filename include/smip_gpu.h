@@ -99,6 +99,11 @@ SMIP_GPU_API int smip_stack_push_frames(smip_stack_t s, const void* frames, int 
  * Only the bispectrum is accumulated (no power spectrum or shift-and-add). */
 SMIP_GPU_API int smip_stack_accumulate_fft(smip_stack_t s, const double* spectra, long count, int on_device);
 
+/* Zeroes the accumulators and the frame count, keeping the device buffers,
+ * so the stack can take a new job (no counterpart in the reference, whose
+ * accumulators live for one smip-cli run). */
+SMIP_GPU_API int smip_stack_reset(smip_stack_t s);
+
 /* Runs the pending partial batch; smip_stack_sync also waits for it. */
 SMIP_GPU_API int smip_stack_flush(smip_stack_t s);
 SMIP_GPU_API int smip_stack_sync(smip_stack_t s);
@@ -174,6 +179,23 @@ SMIP_GPU_API int smip_xcorr_displacement(int device, const double* ref, const do
 /* Hann<double>(xsize, ysize, aperture) (window_function.h:39-46, 70-85),
  * computed on the GPU; SMIP_E_DOMAIN for aperture <= 0. */
 SMIP_GPU_API int smip_hann(int device, double* out, long xsize, long ysize, double aperture);
+
+/* Instrumentation (no counterpart in the reference).
+ * smip_stack_set_timing: record CUDA events around every bispectrum-kernel
+ * launch on the stack's stream.  smip_stack_kernel_time: the summed kernel
+ * time (ms), launches and frames since the last query (waits for the stream).
+ * smip_kernel_launches: kernels this library has launched in this process. */
+SMIP_GPU_API int smip_stack_set_timing(smip_stack_t s, int on);
+SMIP_GPU_API int smip_stack_kernel_time(smip_stack_t s, double* bispec_ms, long* launches, double* frames);
+SMIP_GPU_API long long smip_kernel_launches(void);
+
+/* The device's copy of Bispectrum::get_element's index path (bispectrum.h:
+ * 482-512, 553-589, 324-349) for n tuples idx[4*q..4*q+3] = (ux, uy, vx, vy):
+ * off[q] = packed offset (-1 where the reference throws out_of_range), conj[q]
+ * = 1 where the element is returned conjugated.  The phase-recovery kernel
+ * uses exactly this function; it is exported so its parity can be checked. */
+SMIP_GPU_API int smip_bispec_offsets(int device, long ncols, long nrows, long bdepth, const int* idx, long n,
+                                     long long* off, int* conj);
 
 #ifdef __cplusplus
 }

@@ -47,7 +47,6 @@ struct BCfg {
     static constexpr int BW = J + DE + 2;
     static constexpr int BV = DE + 2;
     static constexpr int THREADS = (KC + 1) * 32;
-    static constexpr int NS = 6;
     static constexpr int WBYTES = KC * BW * 8;
     static constexpr int VBYTES = KC * BV * 8;
     static constexpr int ABYTES = J * 8;
@@ -55,6 +54,8 @@ struct BCfg {
     static constexpr int VOFF = (WBYTES + 127) / 128 * 128;
     static constexpr int AOFF = VOFF + (VBYTES + 127) / 128 * 128;
     static constexpr int STAGE = AOFF + 128;
+    // as many frame stages as ~200 KB of shared memory holds, 4..12
+    static constexpr int NS = (200 * 1024 / STAGE) > 12 ? 12 : ((200 * 1024 / STAGE) < 4 ? 4 : (200 * 1024 / STAGE));
     static constexpr int SMEM = NS * STAGE + 2 * NS * 8;
 };
 
@@ -277,7 +278,7 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
     a.njt = g.H / Cf::J;
     a.ntiles = g.hw * a.njt * Cf::NCH;
     const int grid = a.ntiles < L.num_sms ? a.ntiles : L.num_sms;
-    bispec_accum_kernel<DE><<<grid, Cf::THREADS, Cf::SMEM, st>>>(mW, mV, mA, a);
+    bispec_accum_kernel<DE><<<grid, Cf::THREADS, Cf::SMEM, st>>>(mW, mV, mA, a); note_launches(1);
     return cudaGetLastError();
 }
 
@@ -330,14 +331,14 @@ __global__ void bispec_merge_kernel(float2* __restrict__ Bd, float2* __restrict_
 cudaError_t launch_bispec_normalize(const float2* B, const float2* C, double nframes, long long n, float2* out,
                                     cudaStream_t st)
 {
-    bispec_normalize_kernel<<<2048, 256, 0, st>>>(B, C, nframes, n, out);
+    bispec_normalize_kernel<<<2048, 256, 0, st>>>(B, C, nframes, n, out); note_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_bispec_merge(float2* Bd, float2* Cd, const float2* Bs, const float2* Cs, long long n,
                                 cudaStream_t st)
 {
-    bispec_merge_kernel<<<2048, 256, 0, st>>>(Bd, Cd, Bs, Cs, n);
+    bispec_merge_kernel<<<2048, 256, 0, st>>>(Bd, Cd, Bs, Cs, n); note_launches(1);
     return cudaGetLastError();
 }
 

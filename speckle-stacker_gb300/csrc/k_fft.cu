@@ -222,10 +222,10 @@ cudaError_t launch_row_pass(int dtype, const void* frames, long long fstride, in
     const dim3 grid(g.H / kRowBlock, nframes);
     const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + (kRowBlock / 2) * g.W);
     switch (dtype) {
-    case 0: row_pass_kernel<uint8_t><<<grid, 256, smem, st>>>((const uint8_t*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); break;
-    case 1: row_pass_kernel<uint16_t><<<grid, 256, smem, st>>>((const uint16_t*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); break;
-    case 2: row_pass_kernel<float><<<grid, 256, smem, st>>>((const float*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); break;
-    default: row_pass_kernel<double><<<grid, 256, smem, st>>>((const double*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); break;
+    case 0: row_pass_kernel<uint8_t><<<grid, 256, smem, st>>>((const uint8_t*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); note_launches(1); break;
+    case 1: row_pass_kernel<uint16_t><<<grid, 256, smem, st>>>((const uint16_t*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); note_launches(1); break;
+    case 2: row_pass_kernel<float><<<grid, 256, smem, st>>>((const float*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); note_launches(1); break;
+    default: row_pass_kernel<double><<<grid, 256, smem, st>>>((const double*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); note_launches(1); break;
     }
     return cudaGetLastError();
 }
@@ -238,14 +238,14 @@ cudaError_t launch_col_pass(int mode, float2* Gt, float2* S, const float2* Rbuf,
     const dim3 grid(g.hw, nchunks);
     const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + g.H + 2 * kColLines * g.H) + sizeof(double) * g.H;
     col_pass_kernel<<<grid, 256, smem, st>>>(mode, Gt, S, Rbuf, Rout, Ppart, mode == 1 ? 1 : nframes, fpc,
-                                             skip_xcorr_frame0, g.logH, g.hw, tw);
+                                             skip_xcorr_frame0, g.logH, g.hw, tw); note_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_power_reduce(double* P, const double* Ppart, int nchunks, const Geometry& g, cudaStream_t st)
 {
     const long long n = (long long)g.hw * g.H;
-    power_reduce_kernel<<<grid_for(n, 256), 256, 0, st>>>(P, Ppart, nchunks, n);
+    power_reduce_kernel<<<grid_for(n, 256), 256, 0, st>>>(P, Ppart, nchunks, n); note_launches(1);
     return cudaGetLastError();
 }
 
@@ -259,7 +259,7 @@ cudaError_t launch_xcorr_rows(const float2* Gt, float* corr, int nframes, const 
         if (e != cudaSuccess)
             return e;
     }
-    xcorr_rows_kernel<<<grid, 256, smem, st>>>(Gt, corr, g.logW, g.H, g.hw, tw);
+    xcorr_rows_kernel<<<grid, 256, smem, st>>>(Gt, corr, g.logW, g.H, g.hw, tw); note_launches(1);
     return cudaGetLastError();
 }
 
@@ -267,7 +267,7 @@ cudaError_t launch_import_spectra(const double* spectra, int nframes, const Geom
 {
     const long long n = (long long)g.hw * g.H * nframes;
     import_spectra_kernel<<<grid_for(n, 256), 256, 0, st>>>(reinterpret_cast<const double2*>(spectra), nframes, g.W,
-                                                             g.H, g.hw, S);
+                                                             g.H, g.hw, S); note_launches(1);
     return cudaGetLastError();
 }
 

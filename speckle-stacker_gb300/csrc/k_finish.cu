@@ -115,16 +115,16 @@ cudaError_t launch_finish(const double* Phalf, double pnorm, const double2* phas
 {
     const int n = g.W * g.H;
     const double trigarg = 6.283185307179586476925286766559 / aperture;
-    finish_build_kernel<<<grid_n(n), 256, 0, st>>>(Phalf, pnorm, phases, trigarg, g.W, g.H, Z, power_full);
+    finish_build_kernel<<<grid_n(n), 256, 0, st>>>(Phalf, pnorm, phases, trigarg, g.W, g.H, Z, power_full); note_launches(1);
     const size_t smem = sizeof(double2) * ((1 << (kTwLog - 1)) + 4 * (size_t)(g.W > g.H ? g.W : g.H));
     cudaError_t e = cudaFuncSetAttribute(fft_lines_d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess)
         return e;
     // FFTW_BACKWARD over rows (x) then columns (y)
-    fft_lines_d_kernel<<<(g.H + 3) / 4, 256, smem, st>>>(Z, g.logW, g.H, g.W, 1, +1, tw64);
-    fft_lines_d_kernel<<<(g.W + 3) / 4, 256, smem, st>>>(Z, g.logH, g.W, 1, g.W, +1, tw64);
-    max_abs_kernel<<<1, 1024, 0, st>>>(Z, n, maxbuf);
-    scale_kernel<<<grid_n(n), 256, 0, st>>>(Z, n, maxbuf);
+    fft_lines_d_kernel<<<(g.H + 3) / 4, 256, smem, st>>>(Z, g.logW, g.H, g.W, 1, +1, tw64); note_launches(1);
+    fft_lines_d_kernel<<<(g.W + 3) / 4, 256, smem, st>>>(Z, g.logH, g.W, 1, g.W, +1, tw64); note_launches(1);
+    max_abs_kernel<<<1, 1024, 0, st>>>(Z, n, maxbuf); note_launches(1);
+    scale_kernel<<<grid_n(n), 256, 0, st>>>(Z, n, maxbuf); note_launches(1);
     return cudaGetLastError();
 }
 
@@ -132,14 +132,14 @@ cudaError_t launch_power_full(const double* Phalf, double pnorm, const Geometry&
                               cudaStream_t st)
 {
     const int n = g.W * g.H;
-    finish_build_kernel<<<grid_n(n), 256, 0, st>>>(Phalf, pnorm, nullptr, 0.0, g.W, g.H, nullptr, power_full);
+    finish_build_kernel<<<grid_n(n), 256, 0, st>>>(Phalf, pnorm, nullptr, 0.0, g.W, g.H, nullptr, power_full); note_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_hann(double* out, int W, int H, double aperture, cudaStream_t st)
 {
     const int n = W * H;
-    hann_kernel<<<grid_n(n), 256, 0, st>>>(out, W, H, 6.283185307179586476925286766559 / aperture);
+    hann_kernel<<<grid_n(n), 256, 0, st>>>(out, W, H, 6.283185307179586476925286766559 / aperture); note_launches(1);
     return cudaGetLastError();
 }
 

@@ -7,12 +7,18 @@
 // u and v flagged, |B| > DBL_EPSILON, v inside the bispectrum's v range.
 // Each point may use phases set earlier in the same ring, so the walk is a
 // strict serial chain; the parallelism is inside a point: the (d+1)^2
-// candidate pairs are spread over the 1024 threads of the block and reduced
-// with warp shuffles.
+// candidate pairs are spread over the 1024 threads of the block.
 //
-// Precision: the stored phase map and the final mean / normalisation are
-// FP64; per-pair products use an FP32 mirror of the phase map and FP32
-// phasors (errors ~1e-7 rad per pair, averaged).  B is read through a device
+// Latency structure of one point: the bispectrum gathers depend only on w, not
+// on the chain, so the gathers of the NEXT point are issued before the
+// current point is reduced (software pipelining); the visit list is staged in
+// shared memory; phases of the small v disc live in shared memory.
+//
+// Precision: per-pair products in FP32 from an FP32 mirror of the phase map
+// (~1e-7 rad per pair); the phasor sums are compensated (float-float, ~48-bit)
+// through the thread, warp and block reductions, because at low-consistency
+// points the mean phasor is a large cancellation; the mean, |mean|
+// (consistency) and the stored phase are FP64.  B is read through a device
 // replica of Bispectrum::get_element's index arithmetic, aliasing included.
 // One CTA per job; many jobs (stacks) run in one launch.
 #include "smip_dev.cuh"
@@ -20,6 +26,7 @@
 namespace smip_gpu {
 
 constexpr int kRecoThreads = 1024;
+constexpr int kVisitChunk = 2048;
 
 __device__ __forceinline__ int wrap_idx(int x, int y, int W, int H)
 {
@@ -47,18 +54,42 @@ __device__ __forceinline__ bool unit_phasor(float2 b, float2* out)
     return true;
 }
 
+// float-float accumulation (Knuth two-sum; no multiplies, so no contraction)
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float bh, float bl)
+{
+    const float s = hi + bh;
+    const float bb = s - hi;
+    float e = (hi - (s - bb)) + (bh - bb);
+    e += lo + bl;
+    hi = s + e;
+    lo = e - (hi - s);
+}
+
+struct Slot {
+    float2 b;   // bispectrum element (conjugation applied)
+    int pu;     // index of u in the map, -1 if u is outside the map
+    int ok;     // 1: gather valid, 0: u out of map, -1: get_element would throw
+};
+
+template <int NP>
 __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJob* __restrict__ jobs)
 {
-    extern __shared__ unsigned int flagbits[]; // W*H bits
-    __shared__ float red_r[32], red_i[32];
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ float red[4][32];
     __shared__ int red_n[32];
     const RecoJob J = jobs[blockIdx.x];
     const int W = J.W, H = J.H, De = J.De;
     const int nbits = W * H;
+    const int nside = De + 1, nv = nside * nside;
+    int2* vis = reinterpret_cast<int2*>(smraw);                       // [kVisitChunk]
+    float2* vtab = reinterpret_cast<float2*>(vis + kVisitChunk);      // [nv] phases of the v disc
+    unsigned int* flagbits = reinterpret_cast<unsigned int*>(vtab + nv); // [W*H bits]
     for (int i = threadIdx.x; i < (nbits + 31) / 32; i += blockDim.x)
         flagbits[i] = 0u;
+    for (int i = threadIdx.x; i < nv; i += blockDim.x)
+        vtab[i] = make_float2(0.f, 0.f);
     __syncthreads();
-    // seeds (phasereco.h:42-54)
+    // seeds (phasereco.h:42-54); all lie inside the v disc
     if (threadIdx.x < 5) {
         const int sx[5] = { 0, 1, 0, -1, 0 }, sy[5] = { 0, 0, 1, 0, -1 };
         const int p = wrap_idx(sx[threadIdx.x], sy[threadIdx.x], W, H);
@@ -66,9 +97,9 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
         J.phases[p] = make_double2(1.0, im);
         J.phf[p] = make_float2(1.f, (float)im);
         J.cons[p] = 1.0;
+        vtab[(sy[threadIdx.x] + De / 2) * nside + sx[threadIdx.x] + De / 2] = make_float2(1.f, (float)im);
         atomicOr(&flagbits[p >> 5], 1u << (p & 31));
     }
-    __syncthreads();
 
     BispecDims d;
     const int szW = (W / 2) * 2 + 1, szH = (H / 2) * 2 + 1, szD = De + 1;
@@ -81,100 +112,208 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
     d.base_size = (long long)d.base[0] * d.base[1] * d.base[2] * d.base[3];
     const int pmin0 = -(W >> 1), pmin1 = -(H >> 1);
     const int pmax0 = -W / 2 + W - 1, pmax1 = -H / 2 + H - 1;
-    const int nv = (De + 1) * (De + 1);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-    for (int q = 0; q < J.nvisits; ++q) {
-        const int2 w = J.visits[q];
-        if (w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1)
-            continue;
-        const int pw = wrap_idx(w.x, w.y, W, H);
-        if (flagbits[pw >> 5] & (1u << (pw & 31)))
-            continue;
-        if (abs(w.x) + abs(w.y) <= 1) // phasereco.h:84-86
-            continue;
-        if (w.x < d.mn[0] || w.x > d.mx[0] || w.y < d.mn[1] || w.y > d.mx[1])
-            continue;
-        float sr = 0.f, si = 0.f;
-        int cnt = 0;
-        for (int t = threadIdx.x; t < nv; t += blockDim.x) {
-            const int vx = -De / 2 + t % (De + 1), vy = -De / 2 + t / (De + 1);
-            const int ux = w.x - vx, uy = w.y - vy;
-            if (ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1)
+    // per-thread v candidates (independent of w)
+    int tv[NP], vx[NP], vy[NP], pv[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        tv[p] = threadIdx.x + p * kRecoThreads;
+        vx[p] = -De / 2 + tv[p] % nside;
+        vy[p] = -De / 2 + tv[p] / nside;
+        pv[p] = wrap_idx(vx[p], vy[p], W, H);
+    }
+
+    auto gather = [&](int2 w, Slot* s) {
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            s[p].ok = 0;
+            s[p].pu = -1;
+            s[p].b = make_float2(0.f, 0.f);
+            const int ux = w.x - vx[p], uy = w.y - vy[p];
+            if (tv[p] >= nv || ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1)
                 continue;
-            const int pu = wrap_idx(ux, uy, W, H), pv = wrap_idx(vx, vy, W, H);
-            if (!(flagbits[pu >> 5] & (1u << (pu & 31))) || !(flagbits[pv >> 5] & (1u << (pv & 31))))
-                continue;
+            s[p].pu = wrap_idx(ux, uy, W, H);
             int cj = 0;
-            const long long off = bispec_get_offset(d, ux, uy, vx, vy, &cj);
+            const long long off = bispec_get_offset(d, ux, uy, vx[p], vy[p], &cj);
             if (off < 0) {
-                record_error(J.err, SMIP_DEV_ERR_OUT_OF_RANGE);
+                s[p].ok = -1;
                 continue;
             }
-            float2 b = J.B[off];
+            float2 b = __ldg(&J.B[off]);
             if (cj)
                 b.y = -b.y;
-            float2 bh;
-            if (!unit_phasor(b, &bh))
-                continue;
-            const float2 a = J.phf[pu], c = J.phf[pv];
-            const float2 pp = cmul(a, c);
-            const float2 ph = cmul(pp, make_float2(bh.x, -bh.y));
-            const float r = rsqrtf(ph.x * ph.x + ph.y * ph.y);
-            sr += ph.x * r;
-            si += ph.y * r;
-            ++cnt;
+            s[p].b = b;
+            s[p].ok = 1;
         }
+    };
+
+    Slot cur[NP], nxt[NP];
+    int2 wcur = make_int2(0, 0);
+    __syncthreads();
+    for (int q0 = 0; q0 < J.nvisits; q0 += kVisitChunk) {
+        const int nq = min(kVisitChunk, J.nvisits - q0);
+        __syncthreads();
+        for (int i = threadIdx.x; i < nq; i += blockDim.x)
+            vis[i] = J.visits[q0 + i];
+        __syncthreads();
+        if (q0 == 0) {
+            wcur = vis[0];
+            gather(wcur, cur);
+        }
+        for (int qi = 0; qi < nq; ++qi) {
+            const int q = q0 + qi;
+            // issue the next point's gathers before working on this one
+            if (q + 1 < J.nvisits) {
+                const int2 wn = qi + 1 < nq ? vis[qi + 1] : J.visits[q + 1];
+                gather(wn, nxt);
+                (void)wn;
+            }
+            const int2 w = wcur;
+            bool run = !(w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1);
+            const int pw = run ? wrap_idx(w.x, w.y, W, H) : 0;
+            run = run && !(flagbits[pw >> 5] & (1u << (pw & 31)));
+            run = run && (abs(w.x) + abs(w.y) > 1);                                   // phasereco.h:84
+            run = run && !(w.x < d.mn[0] || w.x > d.mx[0] || w.y < d.mn[1] || w.y > d.mx[1]);
+            if (run) {
+                float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+                int cnt = 0;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            sr += __shfl_xor_sync(0xffffffffu, sr, o);
-            si += __shfl_xor_sync(0xffffffffu, si, o);
-            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-        }
-        if (lane == 0) {
-            red_r[warp] = sr;
-            red_i[warp] = si;
-            red_n[warp] = cnt;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double mr = 0.0, mi = 0.0;
-            int n = 0;
-            for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
-                mr += (double)red_r[i];
-                mi += (double)red_i[i];
-                n += red_n[i];
+                for (int p = 0; p < NP; ++p) {
+                    if (cur[p].ok == 0)
+                        continue;
+                    const int pu = cur[p].pu;
+                    if (!(flagbits[pu >> 5] & (1u << (pu & 31))) || !(flagbits[pv[p] >> 5] & (1u << (pv[p] & 31))))
+                        continue;
+                    if (cur[p].ok < 0) {
+                        record_error(J.err, SMIP_DEV_ERR_OUT_OF_RANGE);
+                        continue;
+                    }
+                    float2 bh;
+                    if (!unit_phasor(cur[p].b, &bh))
+                        continue;
+                    const float2 ph = cmul(cmul(J.phf[pu], vtab[tv[p]]), make_float2(bh.x, -bh.y));
+                    const float r = rsqrtf(ph.x * ph.x + ph.y * ph.y);
+                    ff_add(rh, rl, ph.x * r, 0.f);
+                    ff_add(ih, il, ph.y * r, 0.f);
+                    ++cnt;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
+                    const float c = __shfl_xor_sync(0xffffffffu, ih, o), e = __shfl_xor_sync(0xffffffffu, il, o);
+                    ff_add(rh, rl, a, b);
+                    ff_add(ih, il, c, e);
+                    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+                }
+                if (lane == 0) {
+                    red[0][warp] = rh;
+                    red[1][warp] = rl;
+                    red[2][warp] = ih;
+                    red[3][warp] = il;
+                    red_n[warp] = cnt;
+                }
+                __syncthreads();
+                if (warp == 0) {
+                    rh = red[0][lane];
+                    rl = red[1][lane];
+                    ih = red[2][lane];
+                    il = red[3][lane];
+                    cnt = red_n[lane];
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
+                        const float c = __shfl_xor_sync(0xffffffffu, ih, o), e = __shfl_xor_sync(0xffffffffu, il, o);
+                        ff_add(rh, rl, a, b);
+                        ff_add(ih, il, c, e);
+                        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+                    }
+                    if (lane == 0 && cnt > 0) { // phasereco.h:110-122 in FP64
+                        const double inv_n = 1.0 / (double)cnt;
+                        const double mr = ((double)rh + (double)rl) * inv_n;
+                        const double mi = ((double)ih + (double)il) * inv_n;
+                        const double ab = sqrt(mr * mr + mi * mi);
+                        J.cons[pw] = ab;
+                        double2 ph = make_double2(0.0, 0.0);
+                        if (ab > 2.220446049250313080847263336181640625e-16) {
+                            const double ia = 1.0 / ab;
+                            ph = make_double2(mr * ia, mi * ia);
+                        }
+                        J.phases[pw] = ph;
+                        const float2 pf = make_float2((float)ph.x, (float)ph.y);
+                        J.phf[pw] = pf;
+                        if (abs(w.x) <= De / 2 && abs(w.y) <= De / 2)
+                            vtab[(w.y + De / 2) * nside + w.x + De / 2] = pf;
+                        flagbits[pw >> 5] |= 1u << (pw & 31);
+                    }
+                }
+                __syncthreads();
             }
-            if (n > 0) { // phasereco.h:110-122
-                mr /= (double)n;
-                mi /= (double)n;
-                const double ab = sqrt(mr * mr + mi * mi);
-                J.cons[pw] = ab;
-                double2 ph = make_double2(0.0, 0.0);
-                if (ab > 2.220446049250313080847263336181640625e-16)
-                    ph = make_double2(mr / ab, mi / ab);
-                J.phases[pw] = ph;
-                J.phf[pw] = make_float2((float)ph.x, (float)ph.y);
-                flagbits[pw >> 5] |= 1u << (pw & 31);
-            }
+#pragma unroll
+            for (int p = 0; p < NP; ++p)
+                cur[p] = nxt[p];
+            if (q + 1 < J.nvisits)
+                wcur = qi + 1 < nq ? vis[qi + 1] : J.visits[q + 1];
         }
-        __syncthreads();
     }
+    __syncthreads();
     // export the flag map
     for (int p = threadIdx.x; p < nbits; p += blockDim.x)
         J.flags[p] = (flagbits[p >> 5] >> (p & 31)) & 1u;
 }
 
-cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int max_H, cudaStream_t st)
+// Runs the device get_element index replica on a list of 4-index tuples.
+__global__ void bispec_offset_probe_kernel(BispecDims d, const int4* __restrict__ idx, long long n,
+                                           long long* __restrict__ off, int* __restrict__ conj)
 {
-    const size_t smem = sizeof(unsigned int) * (((size_t)max_W * max_H + 31) / 32);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(phase_reco_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess)
-            return e;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int4 i = idx[q];
+        int cj = 0;
+        off[q] = bispec_get_offset(d, i.x, i.y, i.z, i.w, &cj);
+        conj[q] = off[q] < 0 ? 0 : cj;
     }
-    phase_reco_kernel<<<njobs, kRecoThreads, smem, st>>>(jobs_dev);
+}
+
+cudaError_t launch_offset_probe(const Geometry& g, const int* idx, long long n, long long* off, int* conj,
+                                cudaStream_t st)
+{
+    BispecDims d;
+    const int szW = (g.W / 2) * 2 + 1, szH = (g.H / 2) * 2 + 1, szD = g.De + 1;
+    d.sizes[0] = szW; d.sizes[1] = szH; d.sizes[2] = szD; d.sizes[3] = szD;
+    d.base[0] = szW - szW / 2; d.base[1] = szH; d.base[2] = szD - szD / 2; d.base[3] = szD;
+    for (int k = 0; k < 4; ++k) {
+        d.mn[k] = -(d.sizes[k] / 2);
+        d.mx[k] = d.sizes[k] + d.mn[k] - 1;
+    }
+    d.base_size = (long long)d.base[0] * d.base[1] * d.base[2] * d.base[3];
+    bispec_offset_probe_kernel<<<256, 256, 0, st>>>(d, reinterpret_cast<const int4*>(idx), n, off, conj); note_launches(1);
     return cudaGetLastError();
+}
+
+cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int max_H, int max_De, cudaStream_t st)
+{
+    const int nv = (max_De + 1) * (max_De + 1);
+    const size_t smem = sizeof(int2) * kVisitChunk + sizeof(float2) * nv
+                        + sizeof(unsigned int) * (((size_t)max_W * max_H + 31) / 32);
+    const int np = (nv + kRecoThreads - 1) / kRecoThreads;
+    auto go = [&](auto kern) -> cudaError_t {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess)
+                return e;
+        }
+        kern<<<njobs, kRecoThreads, smem, st>>>(jobs_dev);
+        note_launches(1);
+        return cudaGetLastError();
+    };
+    switch (np) {
+    case 1: return go(phase_reco_kernel<1>);
+    case 2: return go(phase_reco_kernel<2>);
+    case 3: return go(phase_reco_kernel<3>);
+    case 4: return go(phase_reco_kernel<4>);
+    case 5: return go(phase_reco_kernel<5>);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 } // namespace smip_gpu

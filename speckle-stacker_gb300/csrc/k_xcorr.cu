@@ -199,10 +199,10 @@ cudaError_t launch_xcorr_shift(int dtype, const float* corr, const void* frames,
                                cudaStream_t st)
 {
     switch (dtype) {
-    case 0: xcorr_shift_kernel<uint8_t><<<nframes, kShiftThreads, 0, st>>>(corr, (const uint8_t*)frames, fstride, (const uint8_t*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); break;
-    case 1: xcorr_shift_kernel<uint16_t><<<nframes, kShiftThreads, 0, st>>>(corr, (const uint16_t*)frames, fstride, (const uint16_t*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); break;
-    case 2: xcorr_shift_kernel<float><<<nframes, kShiftThreads, 0, st>>>(corr, (const float*)frames, fstride, (const float*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); break;
-    default: xcorr_shift_kernel<double><<<nframes, kShiftThreads, 0, st>>>(corr, (const double*)frames, fstride, (const double*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); break;
+    case 0: xcorr_shift_kernel<uint8_t><<<nframes, kShiftThreads, 0, st>>>(corr, (const uint8_t*)frames, fstride, (const uint8_t*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
+    case 1: xcorr_shift_kernel<uint16_t><<<nframes, kShiftThreads, 0, st>>>(corr, (const uint16_t*)frames, fstride, (const uint16_t*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
+    case 2: xcorr_shift_kernel<float><<<nframes, kShiftThreads, 0, st>>>(corr, (const float*)frames, fstride, (const float*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
+    default: xcorr_shift_kernel<double><<<nframes, kShiftThreads, 0, st>>>(corr, (const double*)frames, fstride, (const double*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
     }
     return cudaGetLastError();
 }
@@ -213,10 +213,10 @@ cudaError_t launch_saa_add(int dtype, void* sum, const void* frames, long long f
     const int n = g.W * g.H;
     const int grid = (n + 255) / 256;
     switch (dtype) {
-    case 0: saa_add_kernel<uint8_t, unsigned long long><<<grid, 256, 0, st>>>((unsigned long long*)sum, (const uint8_t*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); break;
-    case 1: saa_add_kernel<uint16_t, unsigned long long><<<grid, 256, 0, st>>>((unsigned long long*)sum, (const uint16_t*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); break;
-    case 2: saa_add_kernel<float, double><<<grid, 256, 0, st>>>((double*)sum, (const float*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); break;
-    default: saa_add_kernel<double, double><<<grid, 256, 0, st>>>((double*)sum, (const double*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); break;
+    case 0: saa_add_kernel<uint8_t, unsigned long long><<<grid, 256, 0, st>>>((unsigned long long*)sum, (const uint8_t*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
+    case 1: saa_add_kernel<uint16_t, unsigned long long><<<grid, 256, 0, st>>>((unsigned long long*)sum, (const uint16_t*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
+    case 2: saa_add_kernel<float, double><<<grid, 256, 0, st>>>((double*)sum, (const float*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
+    default: saa_add_kernel<double, double><<<grid, 256, 0, st>>>((double*)sum, (const double*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
     }
     return cudaGetLastError();
 }
@@ -224,10 +224,10 @@ cudaError_t launch_saa_add(int dtype, void* sum, const void* frames, long long f
 cudaError_t launch_sumsq(int dtype, const void* frame, long long n, double* out, cudaStream_t st)
 {
     switch (dtype) {
-    case 0: sumsq_kernel<uint8_t><<<1, 1024, 0, st>>>((const uint8_t*)frame, n, out); break;
-    case 1: sumsq_kernel<uint16_t><<<1, 1024, 0, st>>>((const uint16_t*)frame, n, out); break;
-    case 2: sumsq_kernel<float><<<1, 1024, 0, st>>>((const float*)frame, n, out); break;
-    default: sumsq_kernel<double><<<1, 1024, 0, st>>>((const double*)frame, n, out); break;
+    case 0: sumsq_kernel<uint8_t><<<1, 1024, 0, st>>>((const uint8_t*)frame, n, out); note_launches(1); break;
+    case 1: sumsq_kernel<uint16_t><<<1, 1024, 0, st>>>((const uint16_t*)frame, n, out); note_launches(1); break;
+    case 2: sumsq_kernel<float><<<1, 1024, 0, st>>>((const float*)frame, n, out); note_launches(1); break;
+    default: sumsq_kernel<double><<<1, 1024, 0, st>>>((const double*)frame, n, out); note_launches(1); break;
     }
     return cudaGetLastError();
 }

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -46,6 +47,10 @@ static int fail(int code, const std::string& msg)
     } while (0)
 
 extern "C" const char* smip_last_error(void) { return g_last_error.c_str(); }
+
+static std::atomic<long long> g_launches { 0 };
+void smip_gpu::note_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+extern "C" long long smip_kernel_launches(void) { return g_launches.load(); }
 
 extern "C" int smip_version(int* major, int* minor, int* patch)
 {
@@ -228,7 +233,7 @@ struct Reco {
         j.flags = flags;
         j.err = err;
         CUDA_TRY(cudaMemcpyAsync(job, &j, sizeof(RecoJob), cudaMemcpyHostToDevice, st));
-        CUDA_TRY(launch_phase_reco(job, 1, g.W, g.H, st));
+        CUDA_TRY(launch_phase_reco(job, 1, g.W, g.H, g.De, st));
         return SMIP_OK;
     }
     int download(double* ph, unsigned char* fl, double* cs, cudaStream_t st)
@@ -273,6 +278,14 @@ struct smip_stack {
     long nframes = 0;             // frames accumulated (incl. pending)
     int pending = 0;              // frames staged for the next batch
     bool has_ref = false;
+    // optional CUDA-event timing of the bispectrum kernel (on this stream)
+    bool timing = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pool;
+    size_t ev_used = 0;
+    double k2_ms = 0.0;
+    long k2_launches = 0;
+    double k2_frames = 0.0;
+    std::vector<int> ev_frames;
     // device buffers
     float2 *B = nullptr, *C = nullptr, *Bn = nullptr;
     double* P = nullptr;
@@ -304,6 +317,10 @@ struct smip_stack {
         if (ref) cudaFree(ref);
         dfree(ref_sq); dfree(Gt); dfree(S); dfree(R); dfree(corr); dfree(shifts); dfree(err);
         dfree(Z); dfree(pfull); dfree(maxbuf);
+        for (auto& e : ev_pool) {
+            cudaEventDestroy(e.first);
+            cudaEventDestroy(e.second);
+        }
         if (own_stream && st)
             cudaStreamDestroy(st);
     }
@@ -386,8 +403,37 @@ struct smip_stack {
         L.C = C;
         L.err = err;
         L.num_sms = ctx->num_sms;
+        if (timing) {
+            if (ev_used == ev_pool.size()) {
+                cudaEvent_t a, b;
+                CUDA_TRY(cudaEventCreate(&a));
+                CUDA_TRY(cudaEventCreate(&b));
+                ev_pool.emplace_back(a, b);
+                ev_frames.push_back(0);
+            }
+            CUDA_TRY(cudaEventRecord(ev_pool[ev_used].first, st));
+        }
         CUDA_TRY(launch_bispec_accumulate(L, g, st));
+        if (timing) {
+            CUDA_TRY(cudaEventRecord(ev_pool[ev_used].second, st));
+            ev_frames[ev_used] = n;
+            ++ev_used;
+        }
         pending = 0;
+        return SMIP_OK;
+    }
+
+    // folds the recorded event pairs into the totals (stream must be idle)
+    int collect_timing()
+    {
+        for (size_t q = 0; q < ev_used; ++q) {
+            float ms = 0.f;
+            CUDA_TRY(cudaEventElapsedTime(&ms, ev_pool[q].first, ev_pool[q].second));
+            k2_ms += ms;
+            k2_frames += ev_frames[q];
+            ++k2_launches;
+        }
+        ev_used = 0;
         return SMIP_OK;
     }
 };
@@ -465,19 +511,26 @@ extern "C" int smip_stack_push_frames(smip_stack_t s, const void* frames, int dt
         return fail(SMIP_E_INVALID_ARGUMENT, "invalid frame buffer");
     if (s->mode == 2)
         return fail(SMIP_E_INVALID_ARGUMENT, "stack accumulates spectra; frames cannot be mixed in");
-    if (s->dtype >= 0 && s->dtype != dtype)
-        return fail(SMIP_E_INVALID_ARGUMENT, "frame dtype differs from the stack's first frames");
+    if (s->dtype >= 0 && s->dtype != dtype) {
+        if (s->nframes != 0)
+            return fail(SMIP_E_INVALID_ARGUMENT, "frame dtype differs from the stack's first frames");
+        CUDA_TRY(cudaStreamSynchronize(s->st)); // after a reset: new element type
+        cudaFree(s->staging);
+        cudaFree(s->ref);
+        s->staging = s->ref = nullptr;
+        s->dtype = -1;
+    }
     const size_t fbytes = es * s->frame_elems();
     if (stride_bytes == 0)
         stride_bytes = (long)fbytes;
     if ((size_t)stride_bytes < fbytes)
         return fail(SMIP_E_INVALID_ARGUMENT, "frame stride smaller than a frame");
     if (s->dtype < 0) {
-        s->dtype = dtype;
-        s->mode = 1;
         CUDA_TRY(cudaMalloc(&s->staging, fbytes * s->Bf));
         CUDA_TRY(cudaMalloc(&s->ref, fbytes));
+        s->dtype = dtype;
     }
+    s->mode = 1;
     const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     const char* src = static_cast<const char*>(frames);
     long done = 0;
@@ -510,10 +563,9 @@ extern "C" int smip_stack_accumulate_fft(smip_stack_t s, const double* spectra, 
     if (s->mode == 1)
         return fail(SMIP_E_INVALID_ARGUMENT, "stack accumulates frames; spectra cannot be mixed in");
     const size_t sbytes = sizeof(double) * 2 * s->frame_elems();
-    if (s->mode == 0) {
-        s->mode = 2;
+    if (!s->spec_staging)
         CUDA_TRY(cudaMalloc(&s->spec_staging, sbytes * s->Bf));
-    }
+    s->mode = 2;
     const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     long done = 0;
     while (done < count) {
@@ -529,6 +581,53 @@ extern "C" int smip_stack_accumulate_fft(smip_stack_t s, const double* spectra, 
                 return rc;
         }
     }
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_reset(smip_stack_t s)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    if ((rc = s->collect_timing()))
+        return rc;
+    const size_t bs = (size_t)s->g.base_size;
+    CUDA_TRY(cudaMemsetAsync(s->B, 0, sizeof(float2) * bs, s->st));
+    CUDA_TRY(cudaMemsetAsync(s->C, 0, sizeof(float2) * bs, s->st));
+    CUDA_TRY(cudaMemsetAsync(s->P, 0, sizeof(double) * s->half_elems(), s->st));
+    CUDA_TRY(cudaMemsetAsync(s->sum, 0, 8 * s->frame_elems(), s->st));
+    CUDA_TRY(cudaMemsetAsync(s->err, 0, sizeof(int), s->st));
+    s->nframes = 0;
+    s->pending = 0;
+    s->has_ref = false;
+    s->mode = 0;
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_set_timing(smip_stack_t s, int on)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    s->timing = on != 0;
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_kernel_time(smip_stack_t s, double* bispec_ms, long* launches, double* frames)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    if ((rc = s->collect_timing()))
+        return rc;
+    if (bispec_ms) *bispec_ms = s->k2_ms;
+    if (launches) *launches = s->k2_launches;
+    if (frames) *frames = s->k2_frames;
+    s->k2_ms = 0.0;
+    s->k2_launches = 0;
+    s->k2_frames = 0.0;
     return SMIP_OK;
 }
 
@@ -743,7 +842,7 @@ extern "C" int smip_stack_merge(smip_stack_t dst, smip_stack_t src)
     if (src->mode != dst->mode || (src->mode == 1 && src->dtype != dst->dtype))
         return fail(SMIP_E_INVALID_ARGUMENT, "stacks accumulate different inputs");
     CUDA_TRY(launch_bispec_merge(dst->B, dst->C, src->B, src->C, dst->g.base_size, dst->st));
-    add_f64_kernel<<<256, 256, 0, dst->st>>>(dst->P, src->P, (long long)dst->half_elems());
+    add_f64_kernel<<<256, 256, 0, dst->st>>>(dst->P, src->P, (long long)dst->half_elems()); note_launches(1);
     if (dst->mode == 1) {
         if (dst->dtype == SMIP_U8 || dst->dtype == SMIP_U16)
             add_u64_kernel<<<256, 256, 0, dst->st>>>((unsigned long long*)dst->sum, (const unsigned long long*)src->sum,
@@ -751,6 +850,7 @@ extern "C" int smip_stack_merge(smip_stack_t dst, smip_stack_t src)
         else
             add_f64_kernel<<<256, 256, 0, dst->st>>>((double*)dst->sum, (const double*)src->sum,
                                                      (long long)dst->frame_elems());
+        note_launches(1);
         rc = dst->ensure_shift_cap(dst->nframes + src->nframes);
         if (rc)
             return rc;
@@ -882,6 +982,39 @@ extern "C" int smip_xcorr_displacement(int device, const double* refimg, const d
     }
     smip_stack_destroy(s);
     return rc;
+}
+
+extern "C" int smip_bispec_offsets(int device, long ncols, long nrows, long bdepth, const int* idx, long n,
+                                   long long* off, int* conj)
+{
+    // any shape: the index path has no size restriction of its own
+    if (ncols < 1 || nrows < 1 || bdepth < 0 || ncols > (1 << 20) || nrows > (1 << 20) || bdepth > (1 << 20))
+        return fail(SMIP_E_INVALID_ARGUMENT, "invalid bispectrum extents");
+    Geometry g {};
+    g.W = (int)ncols;
+    g.H = (int)nrows;
+    g.De = (int)(bdepth / 2) * 2;
+    if (n < 0 || (n > 0 && (!idx || !off || !conj)))
+        return fail(SMIP_E_INVALID_ARGUMENT, "invalid buffers");
+    if (n == 0)
+        return SMIP_OK;
+    CUDA_TRY(cudaSetDevice(device));
+    int* di = nullptr;
+    long long* doff = nullptr;
+    int* dc = nullptr;
+    cudaError_t e = cudaMalloc(&di, sizeof(int) * 4 * n);
+    if (e == cudaSuccess) e = cudaMalloc(&doff, sizeof(long long) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&dc, sizeof(int) * n);
+    if (e == cudaSuccess) e = cudaMemcpy(di, idx, sizeof(int) * 4 * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_offset_probe(g, di, n, doff, dc, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(off, doff, sizeof(long long) * n, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(conj, dc, sizeof(int) * n, cudaMemcpyDeviceToHost);
+    if (di) cudaFree(di);
+    if (doff) cudaFree(doff);
+    if (dc) cudaFree(dc);
+    if (e != cudaSuccess)
+        return fail(SMIP_E_CUDA, cudaGetErrorString(e));
+    return SMIP_OK;
 }
 
 extern "C" int smip_hann(int device, double* out, long xsize, long ysize, double aperture)

@@ -28,6 +28,9 @@ struct Geometry {
     long long base_size;
 };
 
+// Every kernel launch site reports itself here (process-wide counter).
+void note_launches(int n);
+
 // ---------------------------------------------------------------- launchers
 // All launchers are asynchronous on `st` and return cudaGetLastError().
 
@@ -92,7 +95,10 @@ struct RecoJob {
     unsigned char* flags;
     int* err;
 };
-cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int max_H, cudaStream_t st);
+cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int max_H, int max_De, cudaStream_t st);
+// get_element index replica over a list of (ux, uy, vx, vy) tuples
+cudaError_t launch_offset_probe(const Geometry& g, const int* idx, long long n, long long* off, int* conj,
+                                cudaStream_t st);
 
 // Final image (double precision): Z = sqrt(P_norm) * (phases * hann), inverse
 // FFT, divide by max |.|.  Also writes the full-plane normalised power.

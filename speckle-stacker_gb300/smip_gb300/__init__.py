@@ -110,6 +110,12 @@ def _load():
         "smip_reco_visits": ([C.c_double, ip, C.c_long, lp], C.c_int),
         "smip_xcorr_displacement": ([C.c_int, dp, dp, C.c_long, C.c_long, ip, ip, dp], C.c_int),
         "smip_hann": ([C.c_int, dp, C.c_long, C.c_long, C.c_double], C.c_int),
+        "smip_bispec_offsets": ([C.c_int, C.c_long, C.c_long, C.c_long, ip, C.c_long,
+                                 C.POINTER(C.c_longlong), ip], C.c_int),
+        "smip_stack_reset": ([vp], C.c_int),
+        "smip_stack_set_timing": ([vp, C.c_int], C.c_int),
+        "smip_stack_kernel_time": ([vp, dp, lp, dp], C.c_int),
+        "smip_kernel_launches": ([], C.c_longlong),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -143,6 +149,11 @@ def version():
     a, b, c = C.c_int(), C.c_int(), C.c_int()
     _check(_L().smip_version(C.byref(a), C.byref(b), C.byref(c)))
     return a.value, b.value, c.value
+
+
+def kernel_launches() -> int:
+    """Kernels libsmip_gpu has launched in this process."""
+    return int(_L().smip_kernel_launches())
 
 
 def bispec_base_size(ncols, nrows, depth):
@@ -211,6 +222,20 @@ class Stack:
         if a.ndim == 2:
             a = a[None]
         _check(_L().smip_stack_accumulate_fft(self._h, a.ctypes.data, a.shape[0], 0))
+
+    def reset(self):
+        """Zero the accumulators for a new job (device buffers are kept)."""
+        _check(_L().smip_stack_reset(self._h))
+
+    def set_timing(self, on: bool = True):
+        """Record CUDA events around each bispectrum-kernel launch."""
+        _check(_L().smip_stack_set_timing(self._h, 1 if on else 0))
+
+    def kernel_time(self):
+        """(bispectrum kernel ms, launches, frames) since the last call."""
+        ms, n, fr = C.c_double(), C.c_long(), C.c_double()
+        _check(_L().smip_stack_kernel_time(self._h, C.byref(ms), C.byref(n), C.byref(fr)))
+        return ms.value, n.value, fr.value
 
     def flush(self):
         _check(_L().smip_stack_flush(self._h))
@@ -316,6 +341,16 @@ def reco_visits(reco_radius: float):
     out = np.zeros((n.value, 2), np.int32)
     _check(_L().smip_reco_visits(float(reco_radius), _p(out, C.c_int), n.value, C.byref(n)))
     return out
+
+
+def bispec_offsets(ncols: int, nrows: int, bdepth: int, idx, device: int = 0):
+    """Device get_element index path for (n, 4) tuples -> (offsets int64, conj int32)."""
+    idx = np.ascontiguousarray(idx, np.int32)
+    off = np.zeros(len(idx), np.int64)
+    cj = np.zeros(len(idx), np.int32)
+    _check(_L().smip_bispec_offsets(device, ncols, nrows, bdepth, _p(idx, C.c_int), len(idx),
+                                    off.ctypes.data_as(C.POINTER(C.c_longlong)), _p(cj, C.c_int)))
+    return off, cj
 
 
 def hann(xsize: int, ysize: int, aperture: float, device: int = 0):
