@@ -197,27 +197,56 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
         if (!ok)
             break;
         if (active) {
-            // Kahan-compensated add of the batch partial into (B, C)
-            const long long rowE = (long long)(DE / 2 + 1) * (DE + 1);
-            auto kahan = [&](int j, int l, float2 v) {
+            // Kahan-compensated add of the batch partial into (B, C): every
+            // load is issued before the first store (B and C never alias), so
+            // the tile pays one memory round trip, not one per element.
+            constexpr int rowE = (DE / 2 + 1) * (DE + 1);
+            float2* __restrict__ Bt = p.B + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (DE + 1);
+            float2* __restrict__ Ct = p.C + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (DE + 1);
+            auto off = [&](int j, int l) {
                 const int a1 = j >= 0 ? j : j + H + 1;
                 const int a3 = l >= 0 ? l : l + DE + 1;
-                const long long addr = ((long long)a0 * (H + 1) + a1) * rowE + (long long)a2 * (DE + 1) + a3;
-                float2 b = p.B[addr], c = p.C[addr];
+                return a1 * rowE + a3;
+            };
+            auto kahan = [](float2& b, float2& c, float2 v) {
                 const float yx = v.x - c.x, yy = v.y - c.y;
                 const float tx = b.x + yx, ty = b.y + yy;
                 c.x = (tx - b.x) - yx;
                 c.y = (ty - b.y) - yy;
-                p.B[addr] = make_float2(tx, ty);
-                p.C[addr] = c;
+                b = make_float2(tx, ty);
             };
+            const int oe = off(j0 + (lane & 15), DE / 2);
+            float2 be = make_float2(0.f, 0.f), ce = be;
+            if (lane < 16) {
+                be = Bt[oe];
+                ce = Ct[oe];
+            }
 #pragma unroll
-            for (int a = 0; a < 4; ++a)
+            for (int h = 0; h < 2; ++h) { // two halves keep the register count down
+                int o[2][Cf::TL];
+                float2 bv[2][Cf::TL], cv[2][Cf::TL];
 #pragma unroll
-                for (int b = 0; b < Cf::TL; ++b)
-                    kahan(j0 + jg + 4 * a, -DE / 2 + lg + 8 * b, acc[a][b]);
-            if (lane < 16)
-                kahan(j0 + lane, DE / 2, acce);
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int b = 0; b < Cf::TL; ++b) {
+                        o[a][b] = off(j0 + jg + 4 * (2 * h + a), -DE / 2 + lg + 8 * b);
+                        bv[a][b] = Bt[o[a][b]];
+                        cv[a][b] = Ct[o[a][b]];
+                    }
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int b = 0; b < Cf::TL; ++b) {
+                        kahan(bv[a][b], cv[a][b], acc[2 * h + a][b]);
+                        Bt[o[a][b]] = bv[a][b];
+                        Ct[o[a][b]] = cv[a][b];
+                    }
+            }
+            if (lane < 16) {
+                kahan(be, ce, acce);
+                Bt[oe] = be;
+                Ct[oe] = ce;
+            }
         }
     }
 }

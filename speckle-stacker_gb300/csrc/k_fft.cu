@@ -1,11 +1,23 @@
-// k_fft.cu -- per-frame forward FFT (FP32, shared memory), power spectrum and
-// the cross-correlation transforms.
+// k_fft.cu -- per-frame forward FFT, power spectrum and the
+// cross-correlation transforms.
 //
 // Replaces the FFTW calls of smip-cli/main.cpp:256-259, 271, 296 (forward
-// c2c of each frame), the |F|^2 accumulation of main.cpp:274-279, 300-305 and
-// the r2c / c2r pair of CrossCorrelation::correlate (include/crosscorrel.h:
-// 103-141).  Frames are real, so only the u_x <= 0 half plane is computed;
-// the other half is its complex conjugate mirror.
+// c2c of each frame, FP64 in the reference), the |F|^2 accumulation of
+// main.cpp:274-279, 300-305 and the r2c / c2r pair of
+// CrossCorrelation::correlate (include/crosscorrel.h:103-141).  Frames are
+// real, so only the u_x <= 0 half plane is computed; the other half is its
+// complex conjugate mirror.
+//
+// Precision.  The forward transform runs in float-float arithmetic (~44-bit,
+// smip_dev.cuh) on the FP32 pipes and is rounded to FP32 once at the end, so
+// every frequency bin -- including bins 10^4 x weaker than the frame's
+// energy -- carries FP32 relative accuracy, as the reference's FP64 FFT
+// narrowed to complex<float> (bispectrum.h:399) does.  A plain FP32 FFT loses
+// up to 1e-2 relative accuracy in such bins and 5e-2 in bispectrum elements
+// that are cancellations of them.  The power spectrum is formed from the
+// float-float values in FP64.  The correlation's inverse transform only
+// locates the peak (candidates are re-scored exactly, k_xcorr.cu) and stays
+// FP32.
 //
 // Layout written for the bispectrum kernel (per frame, float2):
 //   S[a][c] = F(x = -a, y = c - H/2),  a in [0, W/2], c in [0, H)
@@ -17,18 +29,30 @@
 
 namespace smip_gpu {
 
-template <typename T> __device__ __forceinline__ float pix_f(const T* p, long long i) { return (float)p[i]; }
+template <typename T> __device__ __forceinline__ float2 pix_df(const T* p, long long i)
+{
+    return make_float2((float)p[i], 0.f); // u8/u16/f32 are exact in FP32
+}
+template <> __device__ __forceinline__ float2 pix_df<double>(const double* p, long long i)
+{
+    const double v = p[i];
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+}
+
+__device__ __forceinline__ float2 df_round(const dfc& v) { return make_float2(v.h.x + v.l.x, v.h.y + v.l.y); }
 
 // ---------------------------------------------------------------- row pass
-// Two real rows per complex FFT of length W (x0 + i x1); the half-spectra are
-// separated afterwards.  Output G'(a, y) = sum_x f(x, y) exp(+2 pi i a x / W).
+// Two real rows per complex FFT of length W (x0 + i x1), float-float; the
+// half-spectra are separated afterwards.  Output G'(a, y) = sum_x f(x, y)
+// exp(+2 pi i a x / W), float-float, stored [f][a][y].
 template <typename T>
 __global__ void __launch_bounds__(256) row_pass_kernel(const T* __restrict__ frames, long long fstride, int logW, int H,
-                                                        int hw, float2* __restrict__ Gt, const float2* __restrict__ tw_g)
+                                                        int hw, dfc* __restrict__ Gt, const dfc* __restrict__ tw_g)
 {
-    extern __shared__ float2 sm[];
-    float2* tw = sm;                              // 2^(kTwLog-1)
-    float2* lines = sm + (1 << (kTwLog - 1));     // [kRowBlock/2][W]
+    extern __shared__ dfc smdf[];
+    dfc* tw = smdf;                                // 2^(kTwLog-1)
+    dfc* lines = smdf + (1 << (kTwLog - 1));       // [kRowBlock/2][W]
     const int W = 1 << logW;
     const int f = blockIdx.y;
     const int y0 = blockIdx.x * kRowBlock;
@@ -36,49 +60,61 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const T* __restrict__ fra
     load_twiddles(tw, tw_g, kTwLog);
     for (int idx = threadIdx.x; idx < kRowBlock * W; idx += blockDim.x) {
         const int r = idx >> logW, x = idx & (W - 1);
-        const float v = pix_f(fr, idx);
-        float* dst = reinterpret_cast<float*>(&lines[(r >> 1) * W + bitrev(x, logW)]);
-        dst[r & 1] = v;
+        const float2 v = pix_df(fr, idx);
+        dfc& d = lines[(r >> 1) * W + bitrev(x, logW)];
+        if (r & 1) {
+            d.h.y = v.x;
+            d.l.y = v.y;
+        } else {
+            d.h.x = v.x;
+            d.l.x = v.y;
+        }
     }
     __syncthreads();
-    fft_stages(lines, logW, kRowBlock / 2, W, tw, kTwLog, -1);
-    float2* out = Gt + (long long)f * hw * H;
+    df_fft_stages(lines, logW, kRowBlock / 2, W, tw, kTwLog, -1);
+    dfc* out = Gt + (long long)f * hw * H;
     for (int idx = threadIdx.x; idx < hw * kRowBlock; idx += blockDim.x) {
         const int a = idx / kRowBlock, r = idx - a * kRowBlock;
-        const float2* Z = lines + (r >> 1) * W;
-        const float2 za = Z[a], zb = Z[(W - a) & (W - 1)];
-        float2 g;
-        if ((r & 1) == 0) // conj of X0 = (Z(a) + conj Z(-a)) / 2
-            g = make_float2(0.5f * (za.x + zb.x), -0.5f * (za.y - zb.y));
-        else // conj of X1 = (Z(a) - conj Z(-a)) / 2i
-            g = make_float2(0.5f * (za.y + zb.y), 0.5f * (za.x - zb.x));
+        const dfc* Z = lines + (r >> 1) * W;
+        const dfc za = Z[a], zb = Z[(W - a) & (W - 1)];
+        dfc g;
+        if ((r & 1) == 0) { // conj of X0 = (Z(a) + conj Z(-a)) / 2
+            df_add(za.h.x, za.l.x, zb.h.x, zb.l.x, g.h.x, g.l.x);
+            df_add(zb.h.y, zb.l.y, -za.h.y, -za.l.y, g.h.y, g.l.y);
+        } else { // conj of X1 = (Z(a) - conj Z(-a)) / 2i
+            df_add(za.h.y, za.l.y, zb.h.y, zb.l.y, g.h.x, g.l.x);
+            df_add(za.h.x, za.l.x, -zb.h.x, -zb.l.x, g.h.y, g.l.y);
+        }
+        g.h.x *= 0.5f; g.l.x *= 0.5f; g.h.y *= 0.5f; g.l.y *= 0.5f;
         out[(long long)a * H + y0 + r] = g;
     }
 }
 
 // ------------------------------------------------------------- column pass
-// One CTA per (a, chunk of frames).  Forward FFT along y gives
-// Fm(a, y) = F(-a, y); writes S, accumulates |F|^2 in FP64 (frame order), and
-// for the correlation computes the inverse y-transform of conj(R) * Fm in
-// place of the input column.
-__global__ void __launch_bounds__(256) col_pass_kernel(int mode, float2* __restrict__ Gt, float2* __restrict__ S,
+// One CTA per (a, chunk of frames).  Float-float forward FFT along y gives
+// Fm(a, y) = F(-a, y); writes S (rounded to FP32), accumulates |F|^2 in FP64
+// (frame order), and for the correlation computes the FP32 inverse
+// y-transform of conj(R) * Fm into T.
+__global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __restrict__ Gt, float2* __restrict__ S,
                                                         const float2* __restrict__ Rbuf, float2* __restrict__ Rout,
-                                                        double* __restrict__ Ppart, int nframes, int fpc,
-                                                        int skip_xcorr_frame0, int logH, int hw,
-                                                        const float2* __restrict__ tw_g)
+                                                        float2* __restrict__ T, double* __restrict__ Ppart,
+                                                        int nframes, int fpc, int skip_xcorr_frame0, int logH, int hw,
+                                                        const dfc* __restrict__ twdf_g, const float2* __restrict__ tw_g)
 {
-    extern __shared__ float2 sm[];
+    extern __shared__ dfc smdf[];
     const int H = 1 << logH;
-    float2* tw = sm;
-    float2* R = tw + (1 << (kTwLog - 1));          // [H]
-    float2* L1 = R + H;                            // [kColLines][H]
-    float2* L2 = L1 + kColLines * H;               // [kColLines][H]
-    double* pacc = reinterpret_cast<double*>(L2 + kColLines * H); // [H]
+    dfc* twd = smdf;                                               // 2^(kTwLog-1)
+    dfc* L1 = twd + (1 << (kTwLog - 1));                           // [kColLines][H]
+    float2* tw = reinterpret_cast<float2*>(L1 + kColLines * H);    // 2^(kTwLog-1)
+    float2* R = tw + (1 << (kTwLog - 1));                          // [H]
+    float2* L2 = R + H;                                            // [kColLines][H]
+    double* pacc = reinterpret_cast<double*>(L2 + kColLines * H);  // [H]
     const int a = blockIdx.x;
     const int chunk = blockIdx.y;
     const int fbeg = chunk * fpc;
     const int fend = min(nframes, fbeg + fpc);
     const long long gstride = (long long)hw * H;
+    load_twiddles(twd, twdf_g, kTwLog);
     load_twiddles(tw, tw_g, kTwLog);
     if (mode == 0)
         for (int y = threadIdx.x; y < H; y += blockDim.x) {
@@ -93,29 +129,30 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, float2* __restr
             L1[l * H + bitrev(y, logH)] = Gt[(f0 + l) * gstride + (long long)a * H + y];
         }
         __syncthreads();
-        fft_stages(L1, logH, nl, H, tw, kTwLog, -1);
+        df_fft_stages(L1, logH, nl, H, twd, kTwLog, -1);
         if (mode == 1) { // reference spectrum only
             for (int y = threadIdx.x; y < H; y += blockDim.x)
-                Rout[(long long)a * H + y] = L1[y];
+                Rout[(long long)a * H + y] = df_round(L1[y]);
             return;
         }
         for (int idx = threadIdx.x; idx < nl * H; idx += blockDim.x) {
             const int l = idx >> logH, c = idx & (H - 1);
-            S[(f0 + l) * gstride + (long long)a * H + c] = L1[l * H + ((c + H / 2) & (H - 1))];
+            S[(f0 + l) * gstride + (long long)a * H + c] = df_round(L1[l * H + ((c + H / 2) & (H - 1))]);
         }
-        // power spectrum, frames in order per element
+        // power spectrum, frames in order per element, from the float-float values
         for (int c = threadIdx.x; c < H; c += blockDim.x) {
             double acc = pacc[c];
             for (int l = 0; l < nl; ++l) {
-                const float2 v = L1[l * H + ((c + H / 2) & (H - 1))];
-                acc += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+                const dfc v = L1[l * H + ((c + H / 2) & (H - 1))];
+                const double re = (double)v.h.x + (double)v.l.x, im = (double)v.h.y + (double)v.l.y;
+                acc += re * re + im * im;
             }
             pacc[c] = acc;
         }
-        // correlation product conj(R) * F, bit-reversed for the inverse FFT
+        // correlation product conj(R) * F in FP32, bit-reversed for the inverse FFT
         for (int idx = threadIdx.x; idx < nl * H; idx += blockDim.x) {
             const int l = idx >> logH, y = idx & (H - 1);
-            const float2 r = R[y], v = L1[l * H + y];
+            const float2 r = R[y], v = df_round(L1[l * H + y]);
             L2[l * H + bitrev(y, logH)] = make_float2(r.x * v.x + r.y * v.y, r.x * v.y - r.y * v.x);
         }
         __syncthreads();
@@ -124,7 +161,7 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, float2* __restr
             const int l = idx >> logH, y = idx & (H - 1);
             if (skip_xcorr_frame0 && f0 + l == 0)
                 continue;
-            Gt[(f0 + l) * gstride + (long long)a * H + y] = L2[l * H + y];
+            T[(f0 + l) * gstride + (long long)a * H + y] = L2[l * H + y];
         }
     }
     __syncthreads();
@@ -216,50 +253,76 @@ static int grid_for(long long n, int block)
     return (int)(g > 4096 ? 4096 : (g < 1 ? 1 : g));
 }
 
-cudaError_t launch_row_pass(int dtype, const void* frames, long long fstride, int nframes, const Geometry& g,
-                            float2* Gt, const float2* tw, cudaStream_t st)
+template <typename K> static cudaError_t allow_smem(K kern, size_t smem)
+{
+    if (smem <= 48 * 1024)
+        return cudaSuccess;
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+cudaError_t launch_row_pass(int dtype, const void* frames, long long fstride, int nframes, const Geometry& g, dfc* Gt,
+                            const dfc* twdf, cudaStream_t st)
 {
     const dim3 grid(g.H / kRowBlock, nframes);
-    const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + (kRowBlock / 2) * g.W);
+    const size_t smem = sizeof(dfc) * ((1 << (kTwLog - 1)) + (kRowBlock / 2) * g.W);
+    cudaError_t e = cudaSuccess;
     switch (dtype) {
-    case 0: row_pass_kernel<uint8_t><<<grid, 256, smem, st>>>((const uint8_t*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); note_launches(1); break;
-    case 1: row_pass_kernel<uint16_t><<<grid, 256, smem, st>>>((const uint16_t*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); note_launches(1); break;
-    case 2: row_pass_kernel<float><<<grid, 256, smem, st>>>((const float*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); note_launches(1); break;
-    default: row_pass_kernel<double><<<grid, 256, smem, st>>>((const double*)frames, fstride, g.logW, g.H, g.hw, Gt, tw); note_launches(1); break;
+    case 0:
+        if ((e = allow_smem(row_pass_kernel<uint8_t>, smem)) != cudaSuccess) return e;
+        row_pass_kernel<uint8_t><<<grid, 256, smem, st>>>((const uint8_t*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf);
+        break;
+    case 1:
+        if ((e = allow_smem(row_pass_kernel<uint16_t>, smem)) != cudaSuccess) return e;
+        row_pass_kernel<uint16_t><<<grid, 256, smem, st>>>((const uint16_t*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf);
+        break;
+    case 2:
+        if ((e = allow_smem(row_pass_kernel<float>, smem)) != cudaSuccess) return e;
+        row_pass_kernel<float><<<grid, 256, smem, st>>>((const float*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf);
+        break;
+    default:
+        if ((e = allow_smem(row_pass_kernel<double>, smem)) != cudaSuccess) return e;
+        row_pass_kernel<double><<<grid, 256, smem, st>>>((const double*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf);
+        break;
     }
+    note_launches(1);
     return cudaGetLastError();
 }
 
-cudaError_t launch_col_pass(int mode, float2* Gt, float2* S, const float2* Rbuf, float2* Rout, double* Ppart,
-                            int nframes, int fpc, int skip_xcorr_frame0, const Geometry& g, const float2* tw,
-                            cudaStream_t st)
+cudaError_t launch_col_pass(int mode, const dfc* Gt, float2* S, const float2* Rbuf, float2* Rout, float2* T,
+                            double* Ppart, int nframes, int fpc, int skip_xcorr_frame0, const Geometry& g,
+                            const dfc* twdf, const float2* tw, cudaStream_t st)
 {
     const int nchunks = mode == 1 ? 1 : (nframes + fpc - 1) / fpc;
     const dim3 grid(g.hw, nchunks);
-    const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + g.H + 2 * kColLines * g.H) + sizeof(double) * g.H;
-    col_pass_kernel<<<grid, 256, smem, st>>>(mode, Gt, S, Rbuf, Rout, Ppart, mode == 1 ? 1 : nframes, fpc,
-                                             skip_xcorr_frame0, g.logH, g.hw, tw); note_launches(1);
+    const size_t smem = sizeof(dfc) * ((1 << (kTwLog - 1)) + kColLines * g.H)
+                        + sizeof(float2) * ((1 << (kTwLog - 1)) + g.H + kColLines * g.H) + sizeof(double) * g.H;
+    cudaError_t e = allow_smem(col_pass_kernel, smem);
+    if (e != cudaSuccess)
+        return e;
+    col_pass_kernel<<<grid, 256, smem, st>>>(mode, Gt, S, Rbuf, Rout, T, Ppart, mode == 1 ? 1 : nframes, fpc,
+                                             skip_xcorr_frame0, g.logH, g.hw, twdf, tw);
+    note_launches(1);
     return cudaGetLastError();
 }
 
 cudaError_t launch_power_reduce(double* P, const double* Ppart, int nchunks, const Geometry& g, cudaStream_t st)
 {
     const long long n = (long long)g.hw * g.H;
-    power_reduce_kernel<<<grid_for(n, 256), 256, 0, st>>>(P, Ppart, nchunks, n); note_launches(1);
+    power_reduce_kernel<<<grid_for(n, 256), 256, 0, st>>>(P, Ppart, nchunks, n);
+    note_launches(1);
     return cudaGetLastError();
 }
 
-cudaError_t launch_xcorr_rows(const float2* Gt, float* corr, int nframes, const Geometry& g, const float2* tw,
+cudaError_t launch_xcorr_rows(const float2* T, float* corr, int nframes, const Geometry& g, const float2* tw,
                               cudaStream_t st)
 {
     const dim3 grid(g.H / kRowBlock, nframes);
     const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + g.hw * kRowBlock + (kRowBlock / 2) * g.W);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(xcorr_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess)
-            return e;
-    }
-    xcorr_rows_kernel<<<grid, 256, smem, st>>>(Gt, corr, g.logW, g.H, g.hw, tw); note_launches(1);
+    cudaError_t e = allow_smem(xcorr_rows_kernel, smem);
+    if (e != cudaSuccess)
+        return e;
+    xcorr_rows_kernel<<<grid, 256, smem, st>>>(T, corr, g.logW, g.H, g.hw, tw);
+    note_launches(1);
     return cudaGetLastError();
 }
 
@@ -267,7 +330,8 @@ cudaError_t launch_import_spectra(const double* spectra, int nframes, const Geom
 {
     const long long n = (long long)g.hw * g.H * nframes;
     import_spectra_kernel<<<grid_for(n, 256), 256, 0, st>>>(reinterpret_cast<const double2*>(spectra), nframes, g.W,
-                                                             g.H, g.hw, S); note_launches(1);
+                                                             g.H, g.hw, S);
+    note_launches(1);
     return cudaGetLastError();
 }
 

@@ -33,23 +33,24 @@ __device__ __forceinline__ int wrap_idx(int x, int y, int W, int H)
     return (x < 0 ? x + W : x) + (y < 0 ? y + H : y) * W;
 }
 
-// unit phasor of B as FP32 without overflow: scale by a power of two first
+// Unit phasor of B in FP32 without overflow (scale by a power of two), and
+// the reference's test |B| > DBL_EPSILON = 2^-52 (phasereco.h:100) decided
+// from the binary exponent, without FP64 arithmetic.
 __device__ __forceinline__ bool unit_phasor(float2 b, float2* out)
 {
     const float m = fmaxf(fabsf(b.x), fabsf(b.y));
-    // |B| > DBL_EPSILON (phasereco.h:100); |B| >= m and |B| <= m*sqrt(2)
-    const double eps = 2.220446049250313080847263336181640625e-16;
-    if ((double)m * 1.4142135623730951 <= eps)
+    if (!(m > 0.f))
         return false;
-    if ((double)m <= eps) {
-        const double bx = b.x, by = b.y;
-        if (!(sqrt(bx * bx + by * by) > eps))
-            return false;
-    }
     int e;
-    frexpf(m, &e);
+    frexpf(m, &e); // m = f * 2^e, f in [0.5, 1)
     const float sx = ldexpf(b.x, -e), sy = ldexpf(b.y, -e);
-    const float r = rsqrtf(sx * sx + sy * sy);
+    const float n2 = sx * sx + sy * sy; // |B|^2 / 4^e, in [0.25, 2)
+    // |B| = 2^e sqrt(n2) with sqrt(n2) in [0.5, sqrt 2)
+    if (e <= -53)
+        return false;
+    if (e == -52 && !(n2 > 1.f))
+        return false;
+    const float r = rsqrtf(n2);
     *out = make_float2(sx * r, sy * r);
     return true;
 }
@@ -67,6 +68,7 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float bh, float bl)
 
 struct Slot {
     float2 b;   // bispectrum element (conjugation applied)
+    float2 pu_ph; // phase of u as read when the gather was issued
     int pu;     // index of u in the map, -1 if u is outside the map
     int ok;     // 1: gather valid, 0: u out of map, -1: get_element would throw
 };
@@ -77,6 +79,8 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ float red[4][32];
     __shared__ int red_n[32];
+    __shared__ int last_pw;
+    __shared__ float2 last_ph;
     const RecoJob J = jobs[blockIdx.x];
     const int W = J.W, H = J.H, De = J.De;
     const int nbits = W * H;
@@ -88,16 +92,18 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
         flagbits[i] = 0u;
     for (int i = threadIdx.x; i < nv; i += blockDim.x)
         vtab[i] = make_float2(0.f, 0.f);
+    if (threadIdx.x == 0)
+        last_pw = -1;
     __syncthreads();
     // seeds (phasereco.h:42-54); all lie inside the v disc
     if (threadIdx.x < 5) {
         const int sx[5] = { 0, 1, 0, -1, 0 }, sy[5] = { 0, 0, 1, 0, -1 };
         const int p = wrap_idx(sx[threadIdx.x], sy[threadIdx.x], W, H);
-        const double im = threadIdx.x < 3 ? 0.0 : -0.0;
-        J.phases[p] = make_double2(1.0, im);
-        J.phf[p] = make_float2(1.f, (float)im);
-        J.cons[p] = 1.0;
-        vtab[(sy[threadIdx.x] + De / 2) * nside + sx[threadIdx.x] + De / 2] = make_float2(1.f, (float)im);
+        const float im = threadIdx.x < 3 ? 0.f : -0.f;
+        J.phf[p] = make_float2(1.f, im);
+        J.sums[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        J.cnt[p] = -1; // seed
+        vtab[(sy[threadIdx.x] + De / 2) * nside + sx[threadIdx.x] + De / 2] = make_float2(1.f, im);
         atomicOr(&flagbits[p >> 5], 1u << (p & 31));
     }
 
@@ -124,12 +130,13 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
         pv[p] = wrap_idx(vx[p], vy[p], W, H);
     }
 
+    // gathers of one point: independent of the chain except phi(u), which
+    // is re-read for the one u that the previous point just set
     auto gather = [&](int2 w, Slot* s) {
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
             s[p].ok = 0;
             s[p].pu = -1;
-            s[p].b = make_float2(0.f, 0.f);
             const int ux = w.x - vx[p], uy = w.y - vy[p];
             if (tv[p] >= nv || ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1)
                 continue;
@@ -144,6 +151,7 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
             if (cj)
                 b.y = -b.y;
             s[p].b = b;
+            s[p].pu_ph = J.phf[s[p].pu];
             s[p].ok = 1;
         }
     };
@@ -163,12 +171,8 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
         }
         for (int qi = 0; qi < nq; ++qi) {
             const int q = q0 + qi;
-            // issue the next point's gathers before working on this one
-            if (q + 1 < J.nvisits) {
-                const int2 wn = qi + 1 < nq ? vis[qi + 1] : J.visits[q + 1];
-                gather(wn, nxt);
-                (void)wn;
-            }
+            if (q + 1 < J.nvisits) // the next point's gathers go out first
+                gather(qi + 1 < nq ? vis[qi + 1] : J.visits[q + 1], nxt);
             const int2 w = wcur;
             bool run = !(w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1);
             const int pw = run ? wrap_idx(w.x, w.y, W, H) : 0;
@@ -176,6 +180,8 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
             run = run && (abs(w.x) + abs(w.y) > 1);                                   // phasereco.h:84
             run = run && !(w.x < d.mn[0] || w.x > d.mx[0] || w.y < d.mn[1] || w.y > d.mx[1]);
             if (run) {
+                const int lpw = last_pw;
+                const float2 lph = last_ph;
                 float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
                 int cnt = 0;
 #pragma unroll
@@ -192,7 +198,8 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
                     float2 bh;
                     if (!unit_phasor(cur[p].b, &bh))
                         continue;
-                    const float2 ph = cmul(cmul(J.phf[pu], vtab[tv[p]]), make_float2(bh.x, -bh.y));
+                    const float2 phu = pu == lpw ? lph : cur[p].pu_ph;
+                    const float2 ph = cmul(cmul(phu, vtab[tv[p]]), make_float2(bh.x, -bh.y));
                     const float r = rsqrtf(ph.x * ph.x + ph.y * ph.y);
                     ff_add(rh, rl, ph.x * r, 0.f);
                     ff_add(ih, il, ph.y * r, 0.f);
@@ -228,23 +235,23 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
                         ff_add(ih, il, c, e);
                         cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
                     }
-                    if (lane == 0 && cnt > 0) { // phasereco.h:110-122 in FP64
-                        const double inv_n = 1.0 / (double)cnt;
-                        const double mr = ((double)rh + (double)rl) * inv_n;
-                        const double mi = ((double)ih + (double)il) * inv_n;
-                        const double ab = sqrt(mr * mr + mi * mi);
-                        J.cons[pw] = ab;
-                        double2 ph = make_double2(0.0, 0.0);
-                        if (ab > 2.220446049250313080847263336181640625e-16) {
-                            const double ia = 1.0 / ab;
-                            ph = make_double2(mr * ia, mi * ia);
+                    if (lane == 0 && cnt > 0) {
+                        // FP32 phase for the chain; FP64 values are formed after the walk
+                        const float s2 = rh * rh + ih * ih;
+                        const float lim = 2.220446049250313e-16f * (float)cnt;
+                        float2 pf = make_float2(0.f, 0.f);
+                        if (s2 > lim * lim) {
+                            const float r = rsqrtf(s2);
+                            pf = make_float2(rh * r, ih * r);
                         }
-                        J.phases[pw] = ph;
-                        const float2 pf = make_float2((float)ph.x, (float)ph.y);
                         J.phf[pw] = pf;
+                        J.sums[pw] = make_float4(rh, rl, ih, il);
+                        J.cnt[pw] = cnt;
                         if (abs(w.x) <= De / 2 && abs(w.y) <= De / 2)
                             vtab[(w.y + De / 2) * nside + w.x + De / 2] = pf;
                         flagbits[pw >> 5] |= 1u << (pw & 31);
+                        last_pw = pw;
+                        last_ph = pf;
                     }
                 }
                 __syncthreads();
@@ -257,9 +264,27 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
         }
     }
     __syncthreads();
-    // export the flag map
-    for (int p = threadIdx.x; p < nbits; p += blockDim.x)
-        J.flags[p] = (flagbits[p >> 5] >> (p & 31)) & 1u;
+    // FP64 mean, consistency and phase of every point (phasereco.h:110-122),
+    // and the flag map
+    for (int p = threadIdx.x; p < nbits; p += blockDim.x) {
+        const unsigned f = (flagbits[p >> 5] >> (p & 31)) & 1u;
+        J.flags[p] = f;
+        if (!f)
+            continue;
+        const int n = J.cnt[p];
+        if (n < 0) { // seed
+            J.phases[p] = make_double2(1.0, J.phf[p].y);
+            J.cons[p] = 1.0;
+            continue;
+        }
+        const float4 s = J.sums[p];
+        const double mr = ((double)s.x + (double)s.y) / (double)n;
+        const double mi = ((double)s.z + (double)s.w) / (double)n;
+        const double ab = sqrt(mr * mr + mi * mi);
+        J.cons[p] = ab;
+        J.phases[p] = ab > 2.220446049250313080847263336181640625e-16 ? make_double2(mr / ab, mi / ab)
+                                                                      : make_double2(0.0, 0.0);
+    }
 }
 
 // Runs the device get_element index replica on a list of 4-index tuples.

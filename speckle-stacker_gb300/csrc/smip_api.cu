@@ -66,6 +66,7 @@ namespace {
 struct DeviceCtx {
     float2* tw32 = nullptr;  // exp(-2 pi i k / 2^kTwLog), k < 2^(kTwLog-1)
     double2* tw64 = nullptr;
+    dfc* twdf = nullptr;     // the same table as float-float (hi, lo)
     int num_sms = 0;
 };
 
@@ -88,10 +89,18 @@ int device_ctx(int dev, DeviceCtx** out)
             t64[k] = make_double2(std::cos(a), -std::sin(a));
             t32[k] = make_float2((float)t64[k].x, (float)t64[k].y);
         }
+        std::vector<dfc> tdf(n);
+        for (int k = 0; k < n; ++k) {
+            const float hx = (float)t64[k].x, hy = (float)t64[k].y;
+            tdf[k].h = make_float2(hx, hy);
+            tdf[k].l = make_float2((float)(t64[k].x - (double)hx), (float)(t64[k].y - (double)hy));
+        }
         CUDA_TRY(cudaMalloc(&c.tw32, sizeof(float2) * n));
         CUDA_TRY(cudaMalloc(&c.tw64, sizeof(double2) * n));
+        CUDA_TRY(cudaMalloc(&c.twdf, sizeof(dfc) * n));
         CUDA_TRY(cudaMemcpy(c.tw32, t32.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
         CUDA_TRY(cudaMemcpy(c.tw64, t64.data(), sizeof(double2) * n, cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(c.twdf, tdf.data(), sizeof(dfc) * n, cudaMemcpyHostToDevice));
         it = g_ctx.emplace(dev, c).first;
     }
     *out = &it->second;
@@ -187,6 +196,8 @@ struct Reco {
     int nvisits = 0;
     double2* phases = nullptr;
     float2* phf = nullptr;
+    float4* sums = nullptr;
+    int* cnt = nullptr;
     double* cons = nullptr;
     unsigned char* flags = nullptr;
     RecoJob* job = nullptr;
@@ -195,6 +206,8 @@ struct Reco {
         dfree(visits);
         dfree(phases);
         dfree(phf);
+        dfree(sums);
+        dfree(cnt);
         dfree(cons);
         dfree(flags);
         dfree(job);
@@ -205,6 +218,8 @@ struct Reco {
         if (!phases) {
             CUDA_TRY(cudaMalloc(&phases, sizeof(double2) * np));
             CUDA_TRY(cudaMalloc(&phf, sizeof(float2) * np));
+            CUDA_TRY(cudaMalloc(&sums, sizeof(float4) * np));
+            CUDA_TRY(cudaMalloc(&cnt, sizeof(int) * np));
             CUDA_TRY(cudaMalloc(&cons, sizeof(double) * np));
             CUDA_TRY(cudaMalloc(&flags, np));
             CUDA_TRY(cudaMalloc(&job, sizeof(RecoJob)));
@@ -229,6 +244,8 @@ struct Reco {
         j.De = g.De;
         j.phases = phases;
         j.phf = phf;
+        j.sums = sums;
+        j.cnt = cnt;
         j.cons = cons;
         j.flags = flags;
         j.err = err;
@@ -295,7 +312,8 @@ struct smip_stack {
     double* spec_staging = nullptr; // spectra input (mode 2)
     void* ref = nullptr;          // raw frame 0
     double* ref_sq = nullptr;
-    float2 *Gt = nullptr, *S = nullptr, *R = nullptr;
+    dfc* Gt = nullptr;            // row-FFT output, float-float
+    float2 *T = nullptr, *S = nullptr, *R = nullptr;
     float* corr = nullptr;
     int* shifts = nullptr;        // all frames, int2
     long shifts_cap = 0;
@@ -315,7 +333,7 @@ struct smip_stack {
         if (staging) cudaFree(staging);
         dfree(spec_staging);
         if (ref) cudaFree(ref);
-        dfree(ref_sq); dfree(Gt); dfree(S); dfree(R); dfree(corr); dfree(shifts); dfree(err);
+        dfree(ref_sq); dfree(Gt); dfree(T); dfree(S); dfree(R); dfree(corr); dfree(shifts); dfree(err);
         dfree(Z); dfree(pfull); dfree(maxbuf);
         for (auto& e : ev_pool) {
             cudaEventDestroy(e.first);
@@ -341,7 +359,8 @@ struct smip_stack {
         CUDA_TRY(cudaMalloc(&Ppart, sizeof(double) * half_elems() * nchunks));
         CUDA_TRY(cudaMalloc(&sum, 8 * frame_elems()));
         CUDA_TRY(cudaMemsetAsync(sum, 0, 8 * frame_elems(), st));
-        CUDA_TRY(cudaMalloc(&Gt, sizeof(float2) * half_elems() * Bf));
+        CUDA_TRY(cudaMalloc(&Gt, sizeof(dfc) * half_elems() * Bf));
+        CUDA_TRY(cudaMalloc(&T, sizeof(float2) * half_elems() * Bf));
         CUDA_TRY(cudaMalloc(&S, sizeof(float2) * half_elems() * Bf));
         CUDA_TRY(cudaMalloc(&R, sizeof(float2) * half_elems()));
         CUDA_TRY(cudaMalloc(&corr, sizeof(float) * frame_elems() * Bf));
@@ -385,12 +404,13 @@ struct smip_stack {
                 CUDA_TRY(cudaMemcpyAsync(ref, staging, dtype_size(dtype) * fe, cudaMemcpyDeviceToDevice, st));
                 CUDA_TRY(launch_sumsq(dtype, ref, (long long)fe, ref_sq, st));
             }
-            CUDA_TRY(launch_row_pass(dtype, staging, (long long)fe, n, g, Gt, ctx->tw32, st));
+            CUDA_TRY(launch_row_pass(dtype, staging, (long long)fe, n, g, Gt, ctx->twdf, st));
             if (first)
-                CUDA_TRY(launch_col_pass(1, Gt, S, R, R, Ppart, 1, fpc, 0, g, ctx->tw32, st));
-            CUDA_TRY(launch_col_pass(0, Gt, S, R, nullptr, Ppart, n, fpc, first ? 1 : 0, g, ctx->tw32, st));
+                CUDA_TRY(launch_col_pass(1, Gt, S, R, R, T, Ppart, 1, fpc, 0, g, ctx->twdf, ctx->tw32, st));
+            CUDA_TRY(launch_col_pass(0, Gt, S, R, nullptr, T, Ppart, n, fpc, first ? 1 : 0, g, ctx->twdf, ctx->tw32,
+                                     st));
             CUDA_TRY(launch_power_reduce(P, Ppart, (n + fpc - 1) / fpc, g, st));
-            CUDA_TRY(launch_xcorr_rows(Gt, corr, n, g, ctx->tw32, st));
+            CUDA_TRY(launch_xcorr_rows(T, corr, n, g, ctx->tw32, st));
             CUDA_TRY(launch_xcorr_shift(dtype, corr, staging, (long long)fe, ref, ref_sq, n, first ? 1 : 0, g,
                                         shifts + 2 * first_index, st));
             CUDA_TRY(launch_saa_add(dtype, sum, staging, (long long)fe, n, first ? 1 : 0, shifts + 2 * first_index, g, st));

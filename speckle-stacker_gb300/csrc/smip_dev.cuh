@@ -59,6 +59,94 @@ __device__ void fft_stages(C* buf, int logn, int nl, int ls, const C* tw, int tw
     }
 }
 
+// ------------------------------------------------ float-float (~44-bit) FFT
+// A value is hi + lo with |lo| <= ulp(hi)/2.  two_sum / two_prod are the
+// error-free transformations of Knuth and Dekker (two_prod via FMA); products
+// drop only the lo*lo term.  Used for the forward frame FFT so that weak
+// frequency bins keep full FP32 relative accuracy after rounding, as an FP64
+// transform narrowed to FP32 would give them.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, float& rh, float& rl)
+{
+    float s, e;
+    two_sum(ah, bh, s, e);
+    e += al + bl;
+    rh = s + e;
+    rl = e - (rh - s);
+}
+
+__device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& rh, float& rl)
+{
+    const float p = ah * bh;
+    float e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, fmaf(al, bh, e));
+    rh = p + e;
+    rl = e - (rh - p);
+}
+
+__device__ __forceinline__ dfc df_cadd(const dfc& a, const dfc& b)
+{
+    dfc r;
+    df_add(a.h.x, a.l.x, b.h.x, b.l.x, r.h.x, r.l.x);
+    df_add(a.h.y, a.l.y, b.h.y, b.l.y, r.h.y, r.l.y);
+    return r;
+}
+
+__device__ __forceinline__ dfc df_csub(const dfc& a, const dfc& b)
+{
+    dfc r;
+    df_add(a.h.x, a.l.x, -b.h.x, -b.l.x, r.h.x, r.l.x);
+    df_add(a.h.y, a.l.y, -b.h.y, -b.l.y, r.h.y, r.l.y);
+    return r;
+}
+
+__device__ __forceinline__ dfc df_cmul(const dfc& a, const dfc& w)
+{
+    float p1h, p1l, p2h, p2l, p3h, p3l, p4h, p4l;
+    df_mul(a.h.x, a.l.x, w.h.x, w.l.x, p1h, p1l);
+    df_mul(a.h.y, a.l.y, w.h.y, w.l.y, p2h, p2l);
+    df_mul(a.h.x, a.l.x, w.h.y, w.l.y, p3h, p3l);
+    df_mul(a.h.y, a.l.y, w.h.x, w.l.x, p4h, p4l);
+    dfc r;
+    df_add(p1h, p1l, -p2h, -p2l, r.h.x, r.l.x);
+    df_add(p3h, p3l, p4h, p4l, r.h.y, r.l.y);
+    return r;
+}
+
+// In-place radix-2 DIT float-float FFT (same contract as fft_stages).
+__device__ inline void df_fft_stages(dfc* buf, int logn, int nl, int ls, const dfc* tw, int twlog, int sign)
+{
+    const int n = 1 << logn;
+    const int nb = nl * (n >> 1);
+    for (int s = 1; s <= logn; ++s) {
+        const int half = 1 << (s - 1);
+        const int tsh = twlog - s;
+        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+            const int line = b >> (logn - 1);
+            const int q = b & ((n >> 1) - 1);
+            const int k = q & (half - 1);
+            const int i0 = ((q >> (s - 1)) << s) + k;
+            dfc w = tw[k << tsh];
+            if (sign > 0) {
+                w.h.y = -w.h.y;
+                w.l.y = -w.l.y;
+            }
+            dfc* L = buf + line * ls;
+            const dfc a = L[i0];
+            const dfc t = df_cmul(L[i0 + half], w);
+            L[i0] = df_cadd(a, t);
+            L[i0 + half] = df_csub(a, t);
+        }
+        __syncthreads();
+    }
+}
+
 // Copies the twiddle table (2^(twlog-1) entries) into shared memory.
 template <typename C>
 __device__ void load_twiddles(C* dst, const C* src, int twlog)

@@ -28,27 +28,32 @@ struct Geometry {
     long long base_size;
 };
 
+// float-float complex value hi + lo (forward-FFT intermediates, twiddles)
+struct dfc {
+    float2 h, l;
+};
+
 // Every kernel launch site reports itself here (process-wide counter).
 void note_launches(int n);
 
 // ---------------------------------------------------------------- launchers
 // All launchers are asynchronous on `st` and return cudaGetLastError().
 
-// frames (dtype) -> G'(a, y) = sum_x f(x,y) exp(+2 pi i a x / W), stored
-// [f][a][y] (float2).  dtype: 0 u8, 1 u16, 2 f32, 3 f64.
+// frames (dtype) -> G'(a, y) = sum_x f(x,y) exp(+2 pi i a x / W), float-float,
+// stored [f][a][y].  dtype: 0 u8, 1 u16, 2 f32, 3 f64.
 cudaError_t launch_row_pass(int dtype, const void* frames, long long frame_stride_elems, int nframes,
-                            const Geometry& g, float2* Gt, const float2* tw, cudaStream_t st);
+                            const Geometry& g, dfc* Gt, const dfc* twdf, cudaStream_t st);
 
-// Column pass.  mode 1: frame 0 only -> Rbuf (the reference spectrum).
-// mode 0: S[f][a][c] = F(-a, c - H/2), power partials, and the inverse column
-// FFT of conj(R)·F for the cross correlation written back into Gt.
-cudaError_t launch_col_pass(int mode, float2* Gt, float2* S, const float2* Rbuf, float2* Rout, double* Ppart,
-                            int nframes, int frames_per_chunk, int skip_xcorr_frame0, const Geometry& g,
-                            const float2* tw, cudaStream_t st);
+// Column pass.  mode 1: frame 0 only -> Rout (the reference spectrum).
+// mode 0: S[f][a][c] = F(-a, c - H/2), power partials, and the FP32 inverse
+// column FFT of conj(R)·F for the cross correlation into T[f][a][y].
+cudaError_t launch_col_pass(int mode, const dfc* Gt, float2* S, const float2* Rbuf, float2* Rout, float2* T,
+                            double* Ppart, int nframes, int frames_per_chunk, int skip_xcorr_frame0,
+                            const Geometry& g, const dfc* twdf, const float2* tw, cudaStream_t st);
 cudaError_t launch_power_reduce(double* P, const double* Ppart, int nchunks, const Geometry& g, cudaStream_t st);
 
 // Row pass of the correlation's inverse transform: corr[f][y][x] (float).
-cudaError_t launch_xcorr_rows(const float2* Gt, float* corr, int nframes, const Geometry& g, const float2* tw,
+cudaError_t launch_xcorr_rows(const float2* T, float* corr, int nframes, const Geometry& g, const float2* tw,
                               cudaStream_t st);
 
 // Integer shift per frame: FP32 correlation peak, candidates re-scored exactly.
@@ -90,7 +95,9 @@ struct RecoJob {
     int nvisits;
     int W, H, De;
     double2* phases;     // W*H, FFT order
-    float2* phf;         // FP32 mirror of phases (scratch)
+    float2* phf;         // FP32 phases used along the chain (scratch)
+    float4* sums;        // per point: float-float phasor sums (re hi, re lo, im hi, im lo)
+    int* cnt;            // per point: number of phasors (-1 for the seeds)
     double* cons;        // W*H
     unsigned char* flags;
     int* err;
