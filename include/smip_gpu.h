@@ -176,6 +176,21 @@ SMIP_GPU_API int smip_reco_visits(double reco_radius, int* ij, long cap, long* c
 SMIP_GPU_API int smip_xcorr_displacement(int device, const double* ref, const double* frame, long ncols,
                                          long nrows, int* dx, int* dy, double* corr);
 
+/* Same shift as smip_xcorr_displacement, for callers that cannot allocate
+ * device memory while they run: acquisition loops that fix their buffers at
+ * start-up (a cudaMalloc can stall the device mid-stream) and plug-ins whose
+ * host application owns device memory through its own pool allocator.  No
+ * counterpart in the reference.  ref, frame: device pointers to ncols x nrows
+ * doubles; shift: device pointer to two ints (x, y), written on `stream`
+ * (a cudaStream_t, or NULL for the default stream).  Allocates nothing: all
+ * intermediates live in one fixed ~3 MB device array inside the library, so
+ * ncols and nrows must be powers of two in [16, 256] (SMIP_E_UNSUPPORTED
+ * otherwise).  The first call on a device looks up that array and uploads
+ * constants, so make it before any stream capture.  Calls share the array:
+ * calls that overlap on the GPU race and must be ordered by the caller. */
+SMIP_GPU_API int smip_xcorr_displacement_noalloc(const double* ref, const double* frame, long ncols, long nrows,
+                                                 int* shift, void* stream);
+
 /* Hann<double>(xsize, ysize, aperture) (window_function.h:39-46, 70-85),
  * computed on the GPU; SMIP_E_DOMAIN for aperture <= 0. */
 SMIP_GPU_API int smip_hann(int device, double* out, long xsize, long ysize, double aperture);

@@ -48,6 +48,8 @@ static int fail(int code, const std::string& msg)
 
 extern "C" const char* smip_last_error(void) { return g_last_error.c_str(); }
 
+void smip_gpu::set_error_message(const std::string& m) { g_last_error = m; }
+
 static std::atomic<long long> g_launches { 0 };
 void smip_gpu::note_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 extern "C" long long smip_kernel_launches(void) { return g_launches.load(); }

@@ -3,6 +3,7 @@
 
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <string>
 
 namespace smip_gpu {
 
@@ -35,6 +36,9 @@ struct dfc {
 
 // Every kernel launch site reports itself here (process-wide counter).
 void note_launches(int n);
+
+// Sets the message smip_last_error() returns on this thread.
+void set_error_message(const std::string& m);
 
 // ---------------------------------------------------------------- launchers
 // All launchers are asynchronous on `st` and return cudaGetLastError().

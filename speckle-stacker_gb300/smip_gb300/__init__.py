@@ -112,6 +112,7 @@ def _load():
         "smip_hann": ([C.c_int, dp, C.c_long, C.c_long, C.c_double], C.c_int),
         "smip_bispec_offsets": ([C.c_int, C.c_long, C.c_long, C.c_long, ip, C.c_long,
                                  C.POINTER(C.c_longlong), ip], C.c_int),
+        "smip_xcorr_displacement_noalloc": ([vp, vp, C.c_long, C.c_long, vp, vp], C.c_int),
         "smip_stack_reset": ([vp], C.c_int),
         "smip_stack_set_timing": ([vp, C.c_int], C.c_int),
         "smip_stack_kernel_time": ([vp, dp, lp, dp], C.c_int),
@@ -341,6 +342,16 @@ def reco_visits(reco_radius: float):
     out = np.zeros((n.value, 2), np.int32)
     _check(_L().smip_reco_visits(float(reco_radius), _p(out, C.c_int), n.value, C.byref(n)))
     return out
+
+
+def xcorr_displacement_noalloc(ref_ptr: int, frame_ptr: int, ncols: int, nrows: int, shift_ptr: int,
+                               stream: int = 0):
+    """Shift of the frame against ref, computed without allocating device
+    memory (for callers that must not allocate while running).  All three
+    pointers are device addresses: ref and frame hold ncols x nrows doubles,
+    shift receives two int32 (x, y) on ``stream``.  Frames up to 256 x 256."""
+    _check(_L().smip_xcorr_displacement_noalloc(C.c_void_p(ref_ptr), C.c_void_p(frame_ptr), ncols, nrows,
+                                                C.c_void_p(shift_ptr), C.c_void_p(stream) if stream else None))
 
 
 def bispec_offsets(ncols: int, nrows: int, bdepth: int, idx, device: int = 0):
