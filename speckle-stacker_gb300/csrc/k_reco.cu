@@ -25,7 +25,7 @@
 
 namespace smip_gpu {
 
-constexpr int kRecoThreads = 1024;
+constexpr int kRecoThreads = 512;
 constexpr int kVisitChunk = 2048;
 
 __device__ __forceinline__ int wrap_idx(int x, int y, int W, int H)
@@ -66,47 +66,17 @@ __device__ __forceinline__ void ff_add(float& hi, float& lo, float bh, float bl)
     lo = e - (hi - s);
 }
 
-struct Slot {
-    float2 b;   // bispectrum element (conjugation applied)
-    float2 pu_ph; // phase of u as read when the gather was issued
-    int pu;     // index of u in the map, -1 if u is outside the map
-    int ok;     // 1: gather valid, 0: u out of map, -1: get_element would throw
-};
-
-template <int NP>
-__global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJob* __restrict__ jobs)
+// ----------------------------------------------------------------- plan
+// The bispectrum side of every pair the walk can use depends only on (w, v),
+// not on the chain: plan[q][t] = unit phasor of B(w_q - v_t, v_t), or
+// (0, 0) when the pair never contributes (u outside the map, |B| <= eps,
+// w skipped by calc_phase), or NaN where Bispectrum::get_element would throw.
+// Fully parallel over (visit, v); the serial chain then only streams rows.
+__global__ void __launch_bounds__(256) reco_plan_kernel(const RecoJob* __restrict__ jobs)
 {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ float red[4][32];
-    __shared__ int red_n[32];
-    __shared__ int last_pw;
-    __shared__ float2 last_ph;
-    const RecoJob J = jobs[blockIdx.x];
+    const RecoJob J = jobs[blockIdx.y];
     const int W = J.W, H = J.H, De = J.De;
-    const int nbits = W * H;
     const int nside = De + 1, nv = nside * nside;
-    int2* vis = reinterpret_cast<int2*>(smraw);                       // [kVisitChunk]
-    float2* vtab = reinterpret_cast<float2*>(vis + kVisitChunk);      // [nv] phases of the v disc
-    unsigned int* flagbits = reinterpret_cast<unsigned int*>(vtab + nv); // [W*H bits]
-    for (int i = threadIdx.x; i < (nbits + 31) / 32; i += blockDim.x)
-        flagbits[i] = 0u;
-    for (int i = threadIdx.x; i < nv; i += blockDim.x)
-        vtab[i] = make_float2(0.f, 0.f);
-    if (threadIdx.x == 0)
-        last_pw = -1;
-    __syncthreads();
-    // seeds (phasereco.h:42-54); all lie inside the v disc
-    if (threadIdx.x < 5) {
-        const int sx[5] = { 0, 1, 0, -1, 0 }, sy[5] = { 0, 0, 1, 0, -1 };
-        const int p = wrap_idx(sx[threadIdx.x], sy[threadIdx.x], W, H);
-        const float im = threadIdx.x < 3 ? 0.f : -0.f;
-        J.phf[p] = make_float2(1.f, im);
-        J.sums[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-        J.cnt[p] = -1; // seed
-        vtab[(sy[threadIdx.x] + De / 2) * nside + sx[threadIdx.x] + De / 2] = make_float2(1.f, im);
-        atomicOr(&flagbits[p >> 5], 1u << (p & 31));
-    }
-
     BispecDims d;
     const int szW = (W / 2) * 2 + 1, szH = (H / 2) * 2 + 1, szD = De + 1;
     d.sizes[0] = szW; d.sizes[1] = szH; d.sizes[2] = szD; d.sizes[3] = szD;
@@ -118,115 +88,167 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
     d.base_size = (long long)d.base[0] * d.base[1] * d.base[2] * d.base[3];
     const int pmin0 = -(W >> 1), pmin1 = -(H >> 1);
     const int pmax0 = -W / 2 + W - 1, pmax1 = -H / 2 + H - 1;
+    const long long total = (long long)J.nvisits * nv;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int q = (int)(e / nv), t = (int)(e - (long long)q * nv);
+        const int2 w = J.visits[q];
+        float2 out = make_float2(0.f, 0.f);
+        const bool wok = !(w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1) && (abs(w.x) + abs(w.y) > 1)
+                         && !(w.x < d.mn[0] || w.x > d.mx[0] || w.y < d.mn[1] || w.y > d.mx[1]);
+        if (wok) {
+            const int vx = -De / 2 + t % nside, vy = -De / 2 + t / nside;
+            const int ux = w.x - vx, uy = w.y - vy;
+            if (!(ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1)) {
+                int cj = 0;
+                const long long off = bispec_get_offset(d, ux, uy, vx, vy, &cj);
+                if (off < 0) {
+                    out = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
+                } else {
+                    float2 b = __ldg(&J.B[off]);
+                    if (cj)
+                        b.y = -b.y;
+                    float2 bh;
+                    if (unit_phasor(b, &bh))
+                        out = bh;
+                }
+            }
+        }
+        J.plan[e] = out;
+    }
+}
+
+// ---------------------------------------------------------------- chain
+__device__ __forceinline__ void cp_async8(void* smem_dst, const void* gmem_src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(smem_dst)), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// One CTA per job walks the spiral.  For the point being reduced the plan row
+// and the phases phi(u) sit in shared memory; the next point's row and phase
+// gathers are already in flight (cp.async, double-buffered), so the serial
+// path per point is: flag checks, two complex products, the reductions.
+__global__ void __launch_bounds__(kRecoThreads, 1) phase_chain_kernel(const RecoJob* __restrict__ jobs)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ float red[3][32];
+    __shared__ int red_n[32];
+    __shared__ int last_pw;
+    __shared__ float2 last_ph;
+    const RecoJob J = jobs[blockIdx.x];
+    const int W = J.W, H = J.H, De = J.De;
+    const int nbits = W * H;
+    const int nside = De + 1, nv = nside * nside;
+    float2* rowbuf = reinterpret_cast<float2*>(smraw);          // [2][nv] plan rows
+    float2* phubuf = rowbuf + 2 * nv;                            // [2][nv] phi(u) gathers
+    float2* vtab = phubuf + 2 * nv;                              // [nv] phases of the v disc
+    int2* vis = reinterpret_cast<int2*>(vtab + nv);              // [kVisitChunk]
+    unsigned int* flagbits = reinterpret_cast<unsigned int*>(vis + kVisitChunk); // [W*H bits]
+    for (int i = threadIdx.x; i < (nbits + 31) / 32; i += blockDim.x)
+        flagbits[i] = 0u;
+    for (int i = threadIdx.x; i < nv; i += blockDim.x)
+        vtab[i] = make_float2(0.f, 0.f);
+    if (threadIdx.x == 0)
+        last_pw = -1;
+    __syncthreads();
+    if (threadIdx.x < 5) { // seeds (phasereco.h:42-54); all inside the v disc
+        const int sx[5] = { 0, 1, 0, -1, 0 }, sy[5] = { 0, 0, 1, 0, -1 };
+        const int p = wrap_idx(sx[threadIdx.x], sy[threadIdx.x], W, H);
+        const float im = threadIdx.x < 3 ? 0.f : -0.f;
+        J.phf[p] = make_float2(1.f, im);
+        J.sums[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        J.cnt[p] = -1;
+        vtab[(sy[threadIdx.x] + De / 2) * nside + sx[threadIdx.x] + De / 2] = make_float2(1.f, im);
+        atomicOr(&flagbits[p >> 5], 1u << (p & 31));
+    }
+    const int pmin0 = -(W >> 1), pmin1 = -(H >> 1);
+    const int pmax0 = -W / 2 + W - 1, pmax1 = -H / 2 + H - 1;
+    const int szW = (W / 2) * 2 + 1, szH = (H / 2) * 2 + 1;
+    const int umn0 = -(szW / 2), umx0 = szW - szW / 2 - 1, umn1 = -(szH / 2), umx1 = szH - szH / 2 - 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-    // per-thread v candidates (independent of w)
-    int tv[NP], vx[NP], vy[NP], pv[NP];
-#pragma unroll
-    for (int p = 0; p < NP; ++p) {
-        tv[p] = threadIdx.x + p * kRecoThreads;
-        vx[p] = -De / 2 + tv[p] % nside;
-        vy[p] = -De / 2 + tv[p] / nside;
-        pv[p] = wrap_idx(vx[p], vy[p], W, H);
-    }
-
-    // gathers of one point: independent of the chain except phi(u), which
-    // is re-read for the one u that the previous point just set
-    auto gather = [&](int2 w, Slot* s) {
-#pragma unroll
-        for (int p = 0; p < NP; ++p) {
-            s[p].ok = 0;
-            s[p].pu = -1;
-            const int ux = w.x - vx[p], uy = w.y - vy[p];
-            if (tv[p] >= nv || ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1)
-                continue;
-            s[p].pu = wrap_idx(ux, uy, W, H);
-            int cj = 0;
-            const long long off = bispec_get_offset(d, ux, uy, vx[p], vy[p], &cj);
-            if (off < 0) {
-                s[p].ok = -1;
-                continue;
-            }
-            float2 b = __ldg(&J.B[off]);
-            if (cj)
-                b.y = -b.y;
-            s[p].b = b;
-            s[p].pu_ph = J.phf[s[p].pu];
-            s[p].ok = 1;
+    // own slots t = threadIdx.x + k * blockDim.x; each thread reads only what it copied
+    auto prefetch = [&](int q, int2 w, int buf) {
+        const float2* row = J.plan + (long long)q * nv;
+        for (int t = threadIdx.x; t < nv; t += blockDim.x) {
+            cp_async8(&rowbuf[buf * nv + t], &row[t]);
+            const int ux = w.x - (-De / 2 + t % nside), uy = w.y - (-De / 2 + t / nside);
+            if (!(ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1))
+                cp_async8(&phubuf[buf * nv + t], &J.phf[wrap_idx(ux, uy, W, H)]);
         }
+        cp_async_commit();
     };
 
-    Slot cur[NP], nxt[NP];
-    int2 wcur = make_int2(0, 0);
     __syncthreads();
+    int2 wcur = J.visits[0];
+    prefetch(0, wcur, 0);
     for (int q0 = 0; q0 < J.nvisits; q0 += kVisitChunk) {
         const int nq = min(kVisitChunk, J.nvisits - q0);
         __syncthreads();
         for (int i = threadIdx.x; i < nq; i += blockDim.x)
             vis[i] = J.visits[q0 + i];
         __syncthreads();
-        if (q0 == 0) {
-            wcur = vis[0];
-            gather(wcur, cur);
-        }
         for (int qi = 0; qi < nq; ++qi) {
             const int q = q0 + qi;
-            if (q + 1 < J.nvisits) // the next point's gathers go out first
-                gather(qi + 1 < nq ? vis[qi + 1] : J.visits[q + 1], nxt);
+            const int buf = q & 1;
+            // this point's copies (issued one point ago) land; only then is the
+            // other buffer free for the next point's copies
+            cp_async_wait_all();
+            int2 wn = make_int2(0, 0);
+            if (q + 1 < J.nvisits) {
+                wn = qi + 1 < nq ? vis[qi + 1] : J.visits[q + 1];
+                prefetch(q + 1, wn, buf ^ 1);
+            }
             const int2 w = wcur;
             bool run = !(w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1);
             const int pw = run ? wrap_idx(w.x, w.y, W, H) : 0;
             run = run && !(flagbits[pw >> 5] & (1u << (pw & 31)));
             run = run && (abs(w.x) + abs(w.y) > 1);                                   // phasereco.h:84
-            run = run && !(w.x < d.mn[0] || w.x > d.mx[0] || w.y < d.mn[1] || w.y > d.mx[1]);
+            run = run && !(w.x < umn0 || w.x > umx0 || w.y < umn1 || w.y > umx1);
             if (run) {
                 const int lpw = last_pw;
                 const float2 lph = last_ph;
-                float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+                float sr = 0.f, si = 0.f;
                 int cnt = 0;
-#pragma unroll
-                for (int p = 0; p < NP; ++p) {
-                    if (cur[p].ok == 0)
+                for (int t = threadIdx.x; t < nv; t += blockDim.x) {
+                    const float2 bh = rowbuf[buf * nv + t];
+                    if (bh.x == 0.f && bh.y == 0.f)
                         continue;
-                    const int pu = cur[p].pu;
-                    if (!(flagbits[pu >> 5] & (1u << (pu & 31))) || !(flagbits[pv[p] >> 5] & (1u << (pv[p] & 31))))
+                    const int vx = -De / 2 + t % nside, vy = -De / 2 + t / nside;
+                    const int pu = wrap_idx(w.x - vx, w.y - vy, W, H), pv = wrap_idx(vx, vy, W, H);
+                    if (!(flagbits[pu >> 5] & (1u << (pu & 31))) || !(flagbits[pv >> 5] & (1u << (pv & 31))))
                         continue;
-                    if (cur[p].ok < 0) {
+                    if (isnan(bh.x)) {
                         record_error(J.err, SMIP_DEV_ERR_OUT_OF_RANGE);
                         continue;
                     }
-                    float2 bh;
-                    if (!unit_phasor(cur[p].b, &bh))
-                        continue;
-                    const float2 phu = pu == lpw ? lph : cur[p].pu_ph;
-                    const float2 ph = cmul(cmul(phu, vtab[tv[p]]), make_float2(bh.x, -bh.y));
+                    const float2 phu = pu == lpw ? lph : phubuf[buf * nv + t];
+                    const float2 ph = cmul(cmul(phu, vtab[t]), make_float2(bh.x, -bh.y));
                     const float r = rsqrtf(ph.x * ph.x + ph.y * ph.y);
-                    ff_add(rh, rl, ph.x * r, 0.f);
-                    ff_add(ih, il, ph.y * r, 0.f);
+                    sr += ph.x * r;
+                    si += ph.y * r;
                     ++cnt;
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
-                    const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
-                    const float c = __shfl_xor_sync(0xffffffffu, ih, o), e = __shfl_xor_sync(0xffffffffu, il, o);
-                    ff_add(rh, rl, a, b);
-                    ff_add(ih, il, c, e);
+                    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+                    si += __shfl_xor_sync(0xffffffffu, si, o);
                     cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
                 }
                 if (lane == 0) {
-                    red[0][warp] = rh;
-                    red[1][warp] = rl;
-                    red[2][warp] = ih;
-                    red[3][warp] = il;
+                    red[0][warp] = sr;
+                    red[1][warp] = si;
                     red_n[warp] = cnt;
                 }
                 __syncthreads();
                 if (warp == 0) {
-                    rh = red[0][lane];
-                    rl = red[1][lane];
-                    ih = red[2][lane];
-                    il = red[3][lane];
-                    cnt = red_n[lane];
+                    // float-float across warps: the mean phasor can be a large cancellation
+                    const int nw = blockDim.x >> 5;
+                    float rh = lane < nw ? red[0][lane] : 0.f, rl = 0.f;
+                    float ih = lane < nw ? red[1][lane] : 0.f, il = 0.f;
+                    cnt = lane < nw ? red_n[lane] : 0;
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) {
                         const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
@@ -256,13 +278,10 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_reco_kernel(const RecoJ
                 }
                 __syncthreads();
             }
-#pragma unroll
-            for (int p = 0; p < NP; ++p)
-                cur[p] = nxt[p];
-            if (q + 1 < J.nvisits)
-                wcur = qi + 1 < nq ? vis[qi + 1] : J.visits[q + 1];
+            wcur = wn;
         }
     }
+    cp_async_wait_all();
     __syncthreads();
     // FP64 mean, consistency and phase of every point (phasereco.h:110-122),
     // and the flag map
@@ -318,27 +337,18 @@ cudaError_t launch_offset_probe(const Geometry& g, const int* idx, long long n, 
 cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int max_H, int max_De, cudaStream_t st)
 {
     const int nv = (max_De + 1) * (max_De + 1);
-    const size_t smem = sizeof(int2) * kVisitChunk + sizeof(float2) * nv
+    reco_plan_kernel<<<dim3(1024, njobs), 256, 0, st>>>(jobs_dev);
+    note_launches(1);
+    const size_t smem = sizeof(float2) * 5 * nv + sizeof(int2) * kVisitChunk
                         + sizeof(unsigned int) * (((size_t)max_W * max_H + 31) / 32);
-    const int np = (nv + kRecoThreads - 1) / kRecoThreads;
-    auto go = [&](auto kern) -> cudaError_t {
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess)
-                return e;
-        }
-        kern<<<njobs, kRecoThreads, smem, st>>>(jobs_dev);
-        note_launches(1);
-        return cudaGetLastError();
-    };
-    switch (np) {
-    case 1: return go(phase_reco_kernel<1>);
-    case 2: return go(phase_reco_kernel<2>);
-    case 3: return go(phase_reco_kernel<3>);
-    case 4: return go(phase_reco_kernel<4>);
-    case 5: return go(phase_reco_kernel<5>);
-    default: return cudaErrorInvalidValue;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(phase_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess)
+            return e;
     }
+    phase_chain_kernel<<<njobs, kRecoThreads, smem, st>>>(jobs_dev);
+    note_launches(1);
+    return cudaGetLastError();
 }
 
 } // namespace smip_gpu

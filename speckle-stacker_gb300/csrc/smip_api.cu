@@ -199,6 +199,7 @@ struct Reco {
     double2* phases = nullptr;
     float2* phf = nullptr;
     float4* sums = nullptr;
+    float2* plan = nullptr;       // nvisits x (De+1)^2 pair phasors
     int* cnt = nullptr;
     double* cons = nullptr;
     unsigned char* flags = nullptr;
@@ -209,6 +210,7 @@ struct Reco {
         dfree(phases);
         dfree(phf);
         dfree(sums);
+        dfree(plan);
         dfree(cnt);
         dfree(cons);
         dfree(flags);
@@ -228,10 +230,14 @@ struct Reco {
         }
         if (radius != R) {
             std::vector<int2> v = reco_visits(radius);
+            CUDA_TRY(cudaStreamSynchronize(st));
             dfree(visits);
+            dfree(plan);
             CUDA_TRY(cudaMalloc(&visits, sizeof(int2) * v.size()));
             CUDA_TRY(cudaMemcpyAsync(visits, v.data(), sizeof(int2) * v.size(), cudaMemcpyHostToDevice, st));
             nvisits = (int)v.size();
+            const size_t nv = (size_t)(g.De + 1) * (g.De + 1);
+            CUDA_TRY(cudaMalloc(&plan, sizeof(float2) * nv * v.size()));
             R = radius;
         }
         CUDA_TRY(cudaMemsetAsync(phases, 0, sizeof(double2) * np, st));
@@ -247,6 +253,7 @@ struct Reco {
         j.phases = phases;
         j.phf = phf;
         j.sums = sums;
+        j.plan = plan;
         j.cnt = cnt;
         j.cons = cons;
         j.flags = flags;

@@ -100,6 +100,7 @@ struct RecoJob {
     int W, H, De;
     double2* phases;     // W*H, FFT order
     float2* phf;         // FP32 phases used along the chain (scratch)
+    float2* plan;        // [nvisits][(De+1)^2] unit phasors of B for every (visit, v)
     float4* sums;        // per point: float-float phasor sums (re hi, re lo, im hi, im lo)
     int* cnt;            // per point: number of phasors (-1 for the seeds)
     double* cons;        // W*H
