@@ -3,31 +3,45 @@
 // Replaces Bispectrum<complex<float>>::accumulate_from_fft (include/
 // bispectrum.h:356-409) for a batch of frames at once.
 //
-// Work decomposition.  The reference's loop runs over u = (i, j) with
-// i in [-W/2, 0], j in [-H/2, H/2-1] and v = (k, l) with k in [-d/2, 0],
-// l in [-d/2, d/2].  A tile is (a0 = -i, 16 consecutive j, a chunk of k rows);
-// its bispectrum elements stay in registers while the frames of the batch
-// stream through shared memory, so the packed bispectrum is read and written
-// once per batch, not once per frame.
+// The reference's loop runs over u = (i, j) with i in [-W/2, 0], j in
+// [-H/2, H/2-1] and v = (k, l) with k in [-d/2, 0], l in [-d/2, d/2].
+// Indices below: a0 = -i, a2 = -k.
 //
-//   warp w            -> one k row (a2 = -k = chunk*KC + w)
-//   lane (jg, lg)     -> j = j0 + jg + 4*tj (tj < 4),  l = -d/2 + lg + 8*tl (tl < d/8)
-//   lanes 0..15       -> also the l = +d/2 column for j = j0 + lane
+// Work decomposition.  A warp task is (a0, a2, 32 consecutive j, one block of
+// up to 32 l values); its triple sums stay in registers while the frames of
+// the batch stream through shared memory, so the packed bispectrum is read and
+// written once per batch, not once per frame.  A CTA has 16 warps (one CTA per
+// SM: every SM sub-partition runs four equally loaded warps) and covers a tile
+// of JT = 32 * NJB consecutive j:
+//   main tile  (a0, j tile, chunk): rows a2 = 1..d/2 in chunks of RPC rows;
+//   row-0 tile (a0 group, j tile):  row a2 = 0 for RPC consecutive a0.
+// Warp w takes j block w % NJB and (l block, row) from w / NJB.
 //
-// With that mapping the 32 lanes of a warp read 11 consecutive F(u+v) words
-// per shared-memory load (conflict-free), and each F(u+v) value held in a
-// register serves up to four triple products.
+//   lane (jg, lg) -> j = jw + jg + 4 a (a < 8),  l = -d/2 + 8 TLW lb + lg + 8 b (b < TLW)
+//   every lane    -> also the l = +d/2 column for j = jw + lane (last l block)
 //
-// Per frame a dedicated producer warp issues three TMA box loads from the
-// S[f][a][c] spectrum layout (k_fft.cu) into a ring of shared-memory stages:
-//   W box: rows a0 + a2 (a2 in the chunk), columns j + l + H/2   -> F(u+v)
-//   V box: rows a2,                        columns l + H/2       -> F(v)
-//   A box: row a0,                         columns j + H/2       -> F(u)
+// Each thread owns 32 triple sums (8 j x 4 l).  Per frame it loads 8 F(u),
+// TLW F(v) and 8 + 2 (TLW - 1) F(u+v) values, 8 bytes each: the lanes of a warp
+// read few distinct words per load (broadcasts), and every F(u+v) value in a
+// register serves up to four triples.  Shared-memory traffic is about 6.5
+// bytes per triple per lane, below the SM's 128 bytes per cycle at the FMA
+// pipe's rate.  Plain FP32 (8 FMA-pipe instructions per triple): packed f32x2
+// forms would need either register moves on the same pipe or twice the
+// shared-memory bytes, and either costs more than it saves.
+//
+// Per frame, three TMA box loads from the S[f][a][c] spectrum layout
+// (k_fft.cu; 8-byte elements) fill one stage of a shared-memory ring:
+//   W box: rows a0 + a2, columns j + l + H/2   -> F(u+v)
+//   V box: rows a2,      columns l + H/2       -> F(v)
+//   A box: row a0,       columns j + H/2       -> F(u)  (row-0 tiles read F(u)
+//          out of their W box, whose rows are the same a0 rows)
 // Out-of-range rows/columns are zero-filled by the TMA unit, which is exactly
-// the reference's guard (bispectrum.h:397-398): those triples add zero.
+// the reference's guard (bispectrum.h:397-398): those triples add zero.  The
+// ring is refilled round robin: the warp that finishes iteration r, r % 16 ==
+// warp, issues iteration r + NS - kLag once every warp has released r - kLag.
 //
 // Accumulation: plain FP32 within a batch (in registers), Kahan-compensated
-// across batches into (B, C) in HBM.  All mbarrier waits are bounded.
+// across batches into (B, C) in HBM.  Every mbarrier wait is bounded.
 #include <cuda.h>
 
 #include "smip_dev.cuh"
@@ -35,28 +49,35 @@
 namespace smip_gpu {
 
 constexpr uint64_t kWaitNs = 2000000000ull; // 2 s
+constexpr int kLag = 2;                     // iterations between a stage's release and its refill
 
 template <int DE>
 struct BCfg {
-    static constexpr int KK = DE / 2 + 1;          // k rows
-    static constexpr int NCH = (KK + 16) / 17;     // k chunks per (a0, j-tile)
-    static constexpr int KC = (KK + NCH - 1) / NCH;
-    static constexpr int J = 16;
-    static constexpr int TL = DE / 8;
-    static constexpr int NWV = 4 + 2 * (TL - 1);   // W values per thread per frame
-    static constexpr int BW = J + DE + 2;
-    static constexpr int BV = DE + 2;
-    static constexpr int THREADS = (KC + 1) * 32;
-    static constexpr int WBYTES = KC * BW * 8;
-    static constexpr int VBYTES = KC * BV * 8;
-    static constexpr int ABYTES = J * 8;
+    static constexpr int ROWS = DE / 2;                    // main rows a2 = 1..d/2
+    static constexpr int TL = DE / 8;                      // 8-wide l groups in [-d/2, d/2)
+    static constexpr int NLB = (TL + 3) / 4;               // l blocks per row
+    static constexpr int TLW = (TL + NLB - 1) / NLB;       // l groups per block
+    static constexpr int RPC = (NLB == 1 && ROWS % 8 == 0) ? 8 : 4; // rows (a0 for row-0 tiles) per tile
+    static constexpr int WARPS = 16;
+    static constexpr int NJB = WARPS / (RPC * NLB);        // 32-wide j blocks per tile
+    static constexpr int JT = 32 * NJB;                    // tile j width
+    static constexpr int THREADS = WARPS * 32;
+    static constexpr int NCHM = ROWS / RPC;                // main chunks per (a0, j tile)
+    static constexpr int NWV = 8 + 2 * (TLW - 1);          // W values per thread per frame
+    static constexpr int BW = JT + DE + 2;                 // W box columns (even start)
+    static constexpr int BV = DE + 2;                      // V box columns (even start)
+    static constexpr int WBYTES = RPC * BW * 8;
+    static constexpr int VBYTES = RPC * BV * 8;
+    static constexpr int ABYTES = JT * 8;
     static constexpr int WOFF = 0;
     static constexpr int VOFF = (WBYTES + 127) / 128 * 128;
     static constexpr int AOFF = VOFF + (VBYTES + 127) / 128 * 128;
-    static constexpr int STAGE = AOFF + 128;
-    // as many frame stages as ~200 KB of shared memory holds, 4..12
-    static constexpr int NS = (200 * 1024 / STAGE) > 12 ? 12 : ((200 * 1024 / STAGE) < 4 ? 4 : (200 * 1024 / STAGE));
-    static constexpr int SMEM = NS * STAGE + 2 * NS * 8;
+    static constexpr int STAGE = AOFF + (ABYTES + 127) / 128 * 128;
+    static constexpr int NSR = (200 * 1024) / STAGE;       // ~200 KB of frame stages
+    static constexpr int NS = NSR > 16 ? 16 : (NSR < 4 ? 4 : NSR);
+    static constexpr int SMEM = NS * STAGE + 2 * NS * 8 + 16;
+    static_assert(RPC * NLB * NJB == WARPS && ROWS % RPC == 0, "task split");
+    static_assert(BW <= 256 && NS > kLag + 1, "box / ring");
 };
 
 struct BispecArgs {
@@ -65,9 +86,49 @@ struct BispecArgs {
     int* err;
     int nframes;
     int H, hw;
-    int njt;      // H / 16
-    int ntiles;
+    int njt;      // j tiles: ceil(H / JT)
+    int nmain;    // main tiles
+    int ntiles;   // main + row-0 tiles
 };
+
+// Tile geometry shared by the TMA issue path and the consumers.
+struct TileInfo {
+    bool row0;
+    int a0;   // main: the tile's a0; row-0: first a0 of the group
+    int j0;
+    int c;    // main: chunk
+};
+
+template <int DE>
+__device__ __forceinline__ TileInfo decode_tile(int t, const BispecArgs& p)
+{
+    using Cf = BCfg<DE>;
+    TileInfo ti;
+    ti.row0 = t >= p.nmain;
+    int jt;
+    if (!ti.row0) {
+        ti.c = t % Cf::NCHM;
+        const int rest = t / Cf::NCHM;
+        jt = rest % p.njt;
+        ti.a0 = rest / p.njt;
+    } else {
+        const int t0 = t - p.nmain;
+        ti.c = 0;
+        jt = t0 % p.njt;
+        ti.a0 = (t0 / p.njt) * Cf::RPC;
+    }
+    ti.j0 = -(p.H / 2) + Cf::JT * jt;
+    return ti;
+}
+
+__device__ __forceinline__ void cmac(float2& acc, float2 a, float2 v, float2 w)
+{
+    // t = a v;  acc += t conj(w)
+    const float tr = a.x * v.x - a.y * v.y;
+    const float ti = a.x * v.y + a.y * v.x;
+    acc.x = fmaf(tr, w.x, fmaf(ti, w.y, acc.x));
+    acc.y = fmaf(ti, w.x, fmaf(-tr, w.y, acc.y));
+}
 
 template <int DE>
 __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
@@ -78,128 +139,148 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + Cf::NS * Cf::STAGE);
     uint64_t* empty = full + Cf::NS;
+    uint32_t* hi_issued = reinterpret_cast<uint32_t*>(empty + Cf::NS); // highest iteration issued + 1
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
         for (int s = 0; s < Cf::NS; ++s) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], Cf::KC);
+            mbar_init(&empty[s], Cf::WARPS);
         }
         fence_mbar_init();
     }
     __syncthreads();
-    const int H = p.H;
-    const int half_h = H / 2;
+    const int half_h = p.H / 2;
+    const int my_tiles = p.ntiles > (int)blockIdx.x ? (p.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const uint32_t total = (uint32_t)my_tiles * (uint32_t)p.nframes;
+    const int cv = (half_h - DE / 2) & ~1;
+    const int offv = (half_h - DE / 2) - cv;
 
-    if (warp == Cf::KC) { // ---------------------------------------- producer
-        if (lane != 0)
-            return;
-        uint32_t it = 0;
-        bool ok = true;
-        for (int t = blockIdx.x; t < p.ntiles && ok; t += gridDim.x) {
-            const int kc = t % Cf::NCH;
-            const int rest = t / Cf::NCH;
-            const int jt = rest % p.njt, a0 = rest / p.njt;
-            const int j0 = -half_h + Cf::J * jt;
-            const int cw = (j0 + half_h - DE / 2) & ~1;
-            const int cv = (half_h - DE / 2) & ~1;
-            for (int f = 0; f < p.nframes; ++f, ++it) {
-                const int s = it % Cf::NS;
-                const uint32_t use = it / Cf::NS;
-                if (use > 0 && !mbar_wait_bounded(&empty[s], (use - 1) & 1, kWaitNs)) {
-                    record_error(p.err, SMIP_DEV_ERR_TIMEOUT);
-                    ok = false;
-                    break;
-                }
-                unsigned char* st = smem + s * Cf::STAGE;
-                mbar_arrive_expect_tx(&full[s], Cf::WBYTES + Cf::VBYTES + Cf::ABYTES);
-                tma_load_3d(st + Cf::WOFF, &tmW, 2 * cw, a0 + kc * Cf::KC, f, &full[s]);
-                tma_load_3d(st + Cf::VOFF, &tmV, 2 * cv, kc * Cf::KC, f, &full[s]);
-                tma_load_3d(st + Cf::AOFF, &tmA, 2 * (j0 + half_h), a0, f, &full[s]);
-            }
+    // issue the loads of iteration r (tile r / nframes, frame r % nframes) into stage r % NS;
+    // box x coordinates are in 8-byte elements and even (16-byte aligned)
+    auto issue = [&](uint32_t r) {
+        const uint32_t k = r / p.nframes;
+        const int f = (int)(r - k * p.nframes);
+        const TileInfo ti = decode_tile<DE>((int)blockIdx.x + (int)k * (int)gridDim.x, p);
+        const int cw = (ti.j0 + half_h - DE / 2) & ~1;
+        const int s = r % Cf::NS;
+        unsigned char* st = smem + s * Cf::STAGE;
+        if (!ti.row0) {
+            mbar_arrive_expect_tx(&full[s], Cf::WBYTES + Cf::VBYTES + Cf::ABYTES);
+            tma_load_3d(st + Cf::WOFF, &tmW, cw, ti.a0 + 1 + ti.c * Cf::RPC, f, &full[s]);
+            tma_load_3d(st + Cf::VOFF, &tmV, cv, 1 + ti.c * Cf::RPC, f, &full[s]);
+            tma_load_3d(st + Cf::AOFF, &tmA, ti.j0 + half_h, ti.a0, f, &full[s]);
+        } else {
+            mbar_arrive_expect_tx(&full[s], Cf::WBYTES + Cf::VBYTES);
+            tma_load_3d(st + Cf::WOFF, &tmW, cw, ti.a0, f, &full[s]);
+            tma_load_3d(st + Cf::VOFF, &tmV, cv, 0, f, &full[s]);
         }
-        // let the last loads land before the block can retire
-        const uint32_t first = it > (uint32_t)Cf::NS ? it - Cf::NS : 0;
-        for (uint32_t q = first; q < it; ++q)
-            mbar_wait_bounded(&full[q % Cf::NS], (q / Cf::NS) & 1, kWaitNs / 4);
-        return;
+    };
+
+    // The first NS - kLag iterations are issued up front; afterwards the warp
+    // that finishes iteration r with r % WARPS == warp issues r + NS - kLag.
+    constexpr uint32_t kAhead = Cf::NS - kLag;
+    if (threadIdx.x == 0) {
+        const uint32_t n0 = total < kAhead ? total : kAhead;
+        for (uint32_t q = 0; q < n0; ++q)
+            issue(q);
+        *hi_issued = n0;
     }
+    uint32_t nr = (uint32_t)warp + kAhead; // this warp's next refill
+    bool stop = false;
+    __syncthreads();
 
-    // ------------------------------------------------------------ consumers
     const int jg = lane & 3, lg = lane >> 2;
-    uint32_t it = 0;
+    const int jb = warp % Cf::NJB;
+    const int lb = (warp / Cf::NJB) % Cf::NLB;
+    const int wr = warp / (Cf::NJB * Cf::NLB); // row inside the tile's boxes
+    const int nb = Cf::TLW < Cf::TL - Cf::TLW * lb ? Cf::TLW : Cf::TL - Cf::TLW * lb; // valid l groups
+    const bool edge = lb == Cf::NLB - 1;
+    uint32_t r = 0;
     bool ok = true;
-    for (int t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
-        const int kc = t % Cf::NCH;
-        const int rest = t / Cf::NCH;
-        const int jt = rest % p.njt, a0 = rest / p.njt;
-        const int j0 = -half_h + Cf::J * jt;
-        const int a2 = kc * Cf::KC + warp;
-        const bool active = a2 < Cf::KK;
-        const int offw = (j0 + half_h - DE / 2) - ((j0 + half_h - DE / 2) & ~1);
-        const int offv = (half_h - DE / 2) - ((half_h - DE / 2) & ~1);
+    for (int k = 0; k < my_tiles && ok; ++k) {
+        const TileInfo ti = decode_tile<DE>((int)blockIdx.x + k * (int)gridDim.x, p);
+        const int a0 = ti.row0 ? ti.a0 + wr : ti.a0;
+        const int a2 = ti.row0 ? 0 : 1 + ti.c * Cf::RPC + wr;
+        const int vrow = ti.row0 ? 0 : wr;
+        const int jw = ti.j0 + 32 * jb; // first j of this warp
+        const int cw = (ti.j0 + half_h - DE / 2) & ~1;
+        const int offw = (ti.j0 + half_h - DE / 2) - cw;
+        // element offsets inside a stage (8-byte units)
+        const int wbase = wr * Cf::BW + offw + 32 * jb;                 // W at (j = jw, l = -d/2)
+        const int vbase = Cf::VOFF / 8 + vrow * Cf::BV + offv;         // V at l = -d/2
+        const int abase = ti.row0 ? wbase + DE / 2 : Cf::AOFF / 8 + 32 * jb; // A at j = jw
 
-        float2 acc[4][Cf::TL];
-        float2 acce = make_float2(0.f, 0.f);
+        float2 acc[8][Cf::TLW];
 #pragma unroll
-        for (int a = 0; a < 4; ++a)
+        for (int a = 0; a < 8; ++a)
 #pragma unroll
-            for (int b = 0; b < Cf::TL; ++b)
+            for (int b = 0; b < Cf::TLW; ++b)
                 acc[a][b] = make_float2(0.f, 0.f);
+        float2 acce = make_float2(0.f, 0.f);
 
-        for (int f = 0; f < p.nframes; ++f, ++it) {
-            const int s = it % Cf::NS;
-            const uint32_t use = it / Cf::NS;
-            if (ok && !mbar_wait_bounded(&full[s], use & 1, kWaitNs)) {
-                record_error(p.err, SMIP_DEV_ERR_TIMEOUT);
+        for (int f = 0; f < p.nframes; ++f, ++r) {
+            const int s = r % Cf::NS;
+            // every lane waits; the warp leaves together if any lane timed out
+            const bool got = mbar_wait_bounded(&full[s], (r / Cf::NS) & 1, kWaitNs);
+            if (!__all_sync(0xffffffffu, got)) {
+                if (lane == 0)
+                    record_error(p.err, SMIP_DEV_ERR_TIMEOUT);
                 ok = false;
-            }
-            if (!ok)
                 break;
-            const unsigned char* st = smem + s * Cf::STAGE;
-            const float2* Wb = reinterpret_cast<const float2*>(st + Cf::WOFF) + warp * Cf::BW + offw;
-            const float2* Vb = reinterpret_cast<const float2*>(st + Cf::VOFF) + warp * Cf::BV + offv;
-            const float2* Ab = reinterpret_cast<const float2*>(st + Cf::AOFF);
-            if (active) {
-                float2 A[4], V[Cf::TL];
+            }
+            const float2* st = reinterpret_cast<const float2*>(smem + s * Cf::STAGE);
+            const float2* Wb = st + wbase + 8 * Cf::TLW * lb;
+            const float2* Vb = st + vbase + 8 * Cf::TLW * lb;
+            const float2* Ab = st + abase;
+
+            float2 A[8], V[Cf::TLW];
 #pragma unroll
-                for (int a = 0; a < 4; ++a)
-                    A[a] = Ab[jg + 4 * a];
+            for (int a = 0; a < 8; ++a)
+                A[a] = Ab[jg + 4 * a];
 #pragma unroll
-                for (int b = 0; b < Cf::TL; ++b)
-                    V[b] = Vb[lg + 8 * b];
+            for (int b = 0; b < Cf::TLW; ++b)
+                V[b] = b < nb ? Vb[lg + 8 * b] : make_float2(0.f, 0.f);
 #pragma unroll
-                for (int m = 0; m < Cf::NWV; ++m) {
-                    const float2 w = Wb[jg + lg + 4 * m];
+            for (int m = 0; m < Cf::NWV; ++m) {
+                const float2 w = Wb[jg + lg + 4 * m];
 #pragma unroll
-                    for (int b = 0; b < Cf::TL; ++b) {
-                        const int a = m - 2 * b;
-                        if (a >= 0 && a < 4) {
-                            // t = F(u) F(v); acc += t * conj F(u+v)
-                            const float tr = A[a].x * V[b].x - A[a].y * V[b].y;
-                            const float ti = A[a].x * V[b].y + A[a].y * V[b].x;
-                            acc[a][b].x = fmaf(tr, w.x, fmaf(ti, w.y, acc[a][b].x));
-                            acc[a][b].y = fmaf(ti, w.x, fmaf(-tr, w.y, acc[a][b].y));
-                        }
-                    }
-                }
-                if (lane < 16) { // l = +d/2 column
-                    const float2 ae = Ab[lane], ve = Vb[DE], we = Wb[DE + lane];
-                    const float tr = ae.x * ve.x - ae.y * ve.y;
-                    const float ti = ae.x * ve.y + ae.y * ve.x;
-                    acce.x = fmaf(tr, we.x, fmaf(ti, we.y, acce.x));
-                    acce.y = fmaf(ti, we.x, fmaf(-tr, we.y, acce.y));
+                for (int b = 0; b < Cf::TLW; ++b) {
+                    const int a = m - 2 * b;
+                    if (a >= 0 && a < 8 && b < nb)
+                        cmac(acc[a][b], A[a], V[b], w);
                 }
             }
+            if (edge) // l = +d/2 column, j = jw + lane
+                cmac(acce, st[abase + lane], st[vbase + DE], st[wbase + DE + lane]);
             __syncwarp();
             if (lane == 0)
                 mbar_arrive(&empty[s]);
+            if (r + kAhead == nr) { // ring refill, round robin over the warps
+                if (!stop && nr < total) {
+                    bool go = true;
+                    if (lane == 0) {
+                        const uint32_t prev = r - kLag; // the iteration that last used the stage
+                        if (r >= (uint32_t)kLag
+                            && !mbar_wait_bounded(&empty[prev % Cf::NS], (prev / Cf::NS) & 1, kWaitNs)) {
+                            record_error(p.err, SMIP_DEV_ERR_TIMEOUT);
+                            go = false;
+                        } else {
+                            issue(nr);
+                            atomicMax(hi_issued, nr + 1);
+                        }
+                    }
+                    stop = !__shfl_sync(0xffffffffu, go, 0);
+                }
+                nr += Cf::WARPS;
+            }
         }
         if (!ok)
             break;
-        if (active) {
-            // Kahan-compensated add of the batch partial into (B, C): every
-            // load is issued before the first store (B and C never alias), so
-            // the tile pays one memory round trip, not one per element.
+        if (a0 < p.hw && jw < half_h) {
+            // Kahan-compensated add of the batch partial into (B, C); within a
+            // j step every load is issued before the first store (B and C never
+            // alias).
+            const int H = p.H;
             constexpr int rowE = (DE / 2 + 1) * (DE + 1);
             float2* __restrict__ Bt = p.B + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (DE + 1);
             float2* __restrict__ Ct = p.C + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (DE + 1);
@@ -215,39 +296,52 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
                 c.y = (ty - b.y) - yy;
                 b = make_float2(tx, ty);
             };
-            const int oe = off(j0 + (lane & 15), DE / 2);
+            // a tile may reach past j = H/2 - 1 when H < JT: those sums are zero and not stored
+            const bool has_e = edge && jw + lane < half_h;
+            const int oe = off(jw + lane, DE / 2);
             float2 be = make_float2(0.f, 0.f), ce = be;
-            if (lane < 16) {
+            if (has_e) {
                 be = Bt[oe];
                 ce = Ct[oe];
             }
 #pragma unroll
-            for (int h = 0; h < 2; ++h) { // two halves keep the register count down
-                int o[2][Cf::TL];
-                float2 bv[2][Cf::TL], cv[2][Cf::TL];
+            for (int a = 0; a < 8; ++a) { // one j at a time keeps the register count down
+                const int j = jw + jg + 4 * a;
+                if (j < half_h) {
+                    int o[Cf::TLW];
+                    float2 bv[Cf::TLW], cvv[Cf::TLW];
 #pragma unroll
-                for (int a = 0; a < 2; ++a)
+                    for (int b = 0; b < Cf::TLW; ++b)
+                        if (b < nb) {
+                            o[b] = off(j, -DE / 2 + 8 * Cf::TLW * lb + lg + 8 * b);
+                            bv[b] = Bt[o[b]];
+                            cvv[b] = Ct[o[b]];
+                        }
 #pragma unroll
-                    for (int b = 0; b < Cf::TL; ++b) {
-                        o[a][b] = off(j0 + jg + 4 * (2 * h + a), -DE / 2 + lg + 8 * b);
-                        bv[a][b] = Bt[o[a][b]];
-                        cv[a][b] = Ct[o[a][b]];
-                    }
-#pragma unroll
-                for (int a = 0; a < 2; ++a)
-#pragma unroll
-                    for (int b = 0; b < Cf::TL; ++b) {
-                        kahan(bv[a][b], cv[a][b], acc[2 * h + a][b]);
-                        Bt[o[a][b]] = bv[a][b];
-                        Ct[o[a][b]] = cv[a][b];
-                    }
+                    for (int b = 0; b < Cf::TLW; ++b)
+                        if (b < nb) {
+                            kahan(bv[b], cvv[b], acc[a][b]);
+                            Bt[o[b]] = bv[b];
+                            Ct[o[b]] = cvv[b];
+                        }
+                }
             }
-            if (lane < 16) {
+            if (has_e) {
                 kahan(be, ce, acce);
                 Bt[oe] = be;
                 Ct[oe] = ce;
             }
         }
+    }
+    // On an early exit (a timed-out wait), loads may still be in flight: only
+    // the last NS issued iterations can be, so wait (bounded) for those to land
+    // before the block retires.
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t hi = *hi_issued;
+        for (uint32_t q = hi > (uint32_t)Cf::NS ? hi - Cf::NS : 0; q < hi; ++q)
+            if (!mbar_wait_bounded(&full[q % Cf::NS], (q / Cf::NS) & 1, kWaitNs / 4))
+                break;
     }
 }
 
@@ -269,17 +363,18 @@ static EncodeTiledFn get_encode()
     return fn;
 }
 
-// S viewed as FLOAT32 [nframes][hw][2H]; box = {2*bw floats, rows, 1 frame}
-static bool make_map(CUtensorMap* m, const float2* S, int nframes, const Geometry& g, int bw, int rows)
+// S viewed as UINT64 (one complex<float> per element) [nframes][hw][H];
+// box = {bcols, brows, 1 frame}.
+static bool make_map(CUtensorMap* m, const float2* S, int nframes, const Geometry& g, int bcols, int brows)
 {
     EncodeTiledFn enc = get_encode();
     if (!enc)
         return false;
-    const cuuint64_t dims[3] = { (cuuint64_t)2 * g.H, (cuuint64_t)g.hw, (cuuint64_t)nframes };
-    const cuuint64_t strides[2] = { (cuuint64_t)2 * g.H * 4, (cuuint64_t)2 * g.H * 4 * g.hw };
-    const cuuint32_t box[3] = { (cuuint32_t)(2 * bw), (cuuint32_t)rows, 1 };
+    const cuuint64_t dims[3] = { (cuuint64_t)g.H, (cuuint64_t)g.hw, (cuuint64_t)nframes };
+    const cuuint64_t strides[2] = { (cuuint64_t)g.H * 8, (cuuint64_t)g.H * 8 * g.hw };
+    const cuuint32_t box[3] = { (cuuint32_t)bcols, (cuuint32_t)brows, 1 };
     const cuuint32_t es[3] = { 1, 1, 1 };
-    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float2*>(S), dims, strides, box, es,
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<float2*>(S), dims, strides, box, es,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE)
         == CUDA_SUCCESS;
@@ -290,8 +385,8 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
 {
     using Cf = BCfg<DE>;
     CUtensorMap mW, mV, mA;
-    if (!make_map(&mW, L.S, L.nframes, g, Cf::BW, Cf::KC) || !make_map(&mV, L.S, L.nframes, g, Cf::BV, Cf::KC)
-        || !make_map(&mA, L.S, L.nframes, g, Cf::J, 1))
+    if (!make_map(&mW, L.S, L.nframes, g, Cf::BW, Cf::RPC) || !make_map(&mV, L.S, L.nframes, g, Cf::BV, Cf::RPC)
+        || !make_map(&mA, L.S, L.nframes, g, Cf::JT, 1))
         return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(bispec_accum_kernel<DE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          Cf::SMEM);
@@ -304,8 +399,9 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
     a.nframes = L.nframes;
     a.H = g.H;
     a.hw = g.hw;
-    a.njt = g.H / Cf::J;
-    a.ntiles = g.hw * a.njt * Cf::NCH;
+    a.njt = (g.H + Cf::JT - 1) / Cf::JT;
+    a.nmain = g.hw * a.njt * Cf::NCHM;
+    a.ntiles = a.nmain + (g.hw + Cf::RPC - 1) / Cf::RPC * a.njt;
     const int grid = a.ntiles < L.num_sms ? a.ntiles : L.num_sms;
     bispec_accum_kernel<DE><<<grid, Cf::THREADS, Cf::SMEM, st>>>(mW, mV, mA, a); note_launches(1);
     return cudaGetLastError();
