@@ -38,7 +38,7 @@
 // Out-of-range rows/columns are zero-filled by the TMA unit, which is exactly
 // the reference's guard (bispectrum.h:397-398): those triples add zero.  The
 // ring is refilled round robin: the warp that finishes iteration r, r % 16 ==
-// warp, issues iteration r + NS - kLag once every warp has released r - kLag.
+// warp, issues iteration r + NS - kLag once every thread has released r - kLag.
 //
 // Accumulation: plain FP32 within a batch (in registers), Kahan-compensated
 // across batches into (B, C) in HBM.  Every mbarrier wait is bounded.
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < Cf::NS; ++s) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], Cf::WARPS);
+            mbar_init(&empty[s], Cf::THREADS); // every consumer thread releases its own reads
         }
         fence_mbar_init();
     }
@@ -252,9 +252,12 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
             }
             if (edge) // l = +d/2 column, j = jw + lane
                 cmac(acce, st[abase + lane], st[vbase + DE], st[wbase + DE + lane]);
+            // Each thread releases the stage itself: its arrive (release
+            // semantics) orders its own shared-memory reads before the refill.
+            // A single arrive per warp after __syncwarp measured unsafe: the
+            // stage was overwritten under the reads of other lanes.
+            mbar_arrive(&empty[s]);
             __syncwarp();
-            if (lane == 0)
-                mbar_arrive(&empty[s]);
             if (r + kAhead == nr) { // ring refill, round robin over the warps
                 if (!stop && nr < total) {
                     bool go = true;
@@ -265,6 +268,8 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
                             record_error(p.err, SMIP_DEV_ERR_TIMEOUT);
                             go = false;
                         } else {
+                            // generic-proxy reads of the stage before the async-proxy (TMA) writes
+                            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                             issue(nr);
                             atomicMax(hi_issued, nr + 1);
                         }

@@ -52,8 +52,9 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const T* __restrict__ fra
 {
     extern __shared__ dfc smdf[];
     dfc* tw = smdf;                                // 2^(kTwLog-1)
-    dfc* lines = smdf + (1 << (kTwLog - 1));       // [kRowBlock/2][W]
+    dfc* lines = smdf + (1 << (kTwLog - 1));       // [kRowBlock/2][pad8(W)]
     const int W = 1 << logW;
+    const int LW = pad8(W);
     const int f = blockIdx.y;
     const int y0 = blockIdx.x * kRowBlock;
     const T* fr = frames + (long long)f * fstride + (long long)y0 * W;
@@ -61,7 +62,7 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const T* __restrict__ fra
     for (int idx = threadIdx.x; idx < kRowBlock * W; idx += blockDim.x) {
         const int r = idx >> logW, x = idx & (W - 1);
         const float2 v = pix_df(fr, idx);
-        dfc& d = lines[(r >> 1) * W + bitrev(x, logW)];
+        dfc& d = lines[(r >> 1) * LW + pad8(bitrev(x, logW))];
         if (r & 1) {
             d.h.y = v.x;
             d.l.y = v.y;
@@ -71,12 +72,12 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const T* __restrict__ fra
         }
     }
     __syncthreads();
-    df_fft_stages(lines, logW, kRowBlock / 2, W, tw, kTwLog, -1);
+    fft_passes(lines, logW, kRowBlock / 2, LW, tw, kTwLog, -1);
     dfc* out = Gt + (long long)f * hw * H;
     for (int idx = threadIdx.x; idx < hw * kRowBlock; idx += blockDim.x) {
         const int a = idx / kRowBlock, r = idx - a * kRowBlock;
-        const dfc* Z = lines + (r >> 1) * W;
-        const dfc za = Z[a], zb = Z[(W - a) & (W - 1)];
+        const dfc* Z = lines + (r >> 1) * LW;
+        const dfc za = Z[pad8(a)], zb = Z[pad8((W - a) & (W - 1))];
         dfc g;
         if ((r & 1) == 0) { // conj of X0 = (Z(a) + conj Z(-a)) / 2
             df_add(za.h.x, za.l.x, zb.h.x, zb.l.x, g.h.x, g.l.x);
@@ -104,11 +105,12 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __re
     extern __shared__ dfc smdf[];
     const int H = 1 << logH;
     dfc* twd = smdf;                                               // 2^(kTwLog-1)
-    dfc* L1 = twd + (1 << (kTwLog - 1));                           // [kColLines][H]
-    float2* tw = reinterpret_cast<float2*>(L1 + kColLines * H);    // 2^(kTwLog-1)
+    const int LH = pad8(H);                                        // padded line length
+    dfc* L1 = twd + (1 << (kTwLog - 1));                           // [kColLines][LH]
+    float2* tw = reinterpret_cast<float2*>(L1 + kColLines * LH);   // 2^(kTwLog-1)
     float2* R = tw + (1 << (kTwLog - 1));                          // [H]
-    float2* L2 = R + H;                                            // [kColLines][H]
-    double* pacc = reinterpret_cast<double*>(L2 + kColLines * H);  // [H]
+    float2* L2 = R + H;                                            // [kColLines][LH]
+    double* pacc = reinterpret_cast<double*>(L2 + kColLines * LH); // [H]
     const int a = blockIdx.x;
     const int chunk = blockIdx.y;
     const int fbeg = chunk * fpc;
@@ -126,24 +128,24 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __re
         __syncthreads();
         for (int idx = threadIdx.x; idx < nl * H; idx += blockDim.x) {
             const int l = idx >> logH, y = idx & (H - 1);
-            L1[l * H + bitrev(y, logH)] = Gt[(f0 + l) * gstride + (long long)a * H + y];
+            L1[l * LH + pad8(bitrev(y, logH))] = Gt[(f0 + l) * gstride + (long long)a * H + y];
         }
         __syncthreads();
-        df_fft_stages(L1, logH, nl, H, twd, kTwLog, -1);
+        fft_passes(L1, logH, nl, LH, twd, kTwLog, -1);
         if (mode == 1) { // reference spectrum only
             for (int y = threadIdx.x; y < H; y += blockDim.x)
-                Rout[(long long)a * H + y] = df_round(L1[y]);
+                Rout[(long long)a * H + y] = df_round(L1[pad8(y)]);
             return;
         }
         for (int idx = threadIdx.x; idx < nl * H; idx += blockDim.x) {
             const int l = idx >> logH, c = idx & (H - 1);
-            S[(f0 + l) * gstride + (long long)a * H + c] = df_round(L1[l * H + ((c + H / 2) & (H - 1))]);
+            S[(f0 + l) * gstride + (long long)a * H + c] = df_round(L1[l * LH + pad8((c + H / 2) & (H - 1))]);
         }
         // power spectrum, frames in order per element, from the float-float values
         for (int c = threadIdx.x; c < H; c += blockDim.x) {
             double acc = pacc[c];
             for (int l = 0; l < nl; ++l) {
-                const dfc v = L1[l * H + ((c + H / 2) & (H - 1))];
+                const dfc v = L1[l * LH + pad8((c + H / 2) & (H - 1))];
                 const double re = (double)v.h.x + (double)v.l.x, im = (double)v.h.y + (double)v.l.y;
                 acc += re * re + im * im;
             }
@@ -152,16 +154,16 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __re
         // correlation product conj(R) * F in FP32, bit-reversed for the inverse FFT
         for (int idx = threadIdx.x; idx < nl * H; idx += blockDim.x) {
             const int l = idx >> logH, y = idx & (H - 1);
-            const float2 r = R[y], v = df_round(L1[l * H + y]);
-            L2[l * H + bitrev(y, logH)] = make_float2(r.x * v.x + r.y * v.y, r.x * v.y - r.y * v.x);
+            const float2 r = R[y], v = df_round(L1[l * LH + pad8(y)]);
+            L2[l * LH + pad8(bitrev(y, logH))] = make_float2(r.x * v.x + r.y * v.y, r.x * v.y - r.y * v.x);
         }
         __syncthreads();
-        fft_stages(L2, logH, nl, H, tw, kTwLog, +1);
+        fft_passes(L2, logH, nl, LH, tw, kTwLog, +1);
         for (int idx = threadIdx.x; idx < nl * H; idx += blockDim.x) {
             const int l = idx >> logH, y = idx & (H - 1);
             if (skip_xcorr_frame0 && f0 + l == 0)
                 continue;
-            T[(f0 + l) * gstride + (long long)a * H + y] = L2[l * H + y];
+            T[(f0 + l) * gstride + (long long)a * H + y] = L2[l * LH + pad8(y)];
         }
     }
     __syncthreads();
@@ -191,7 +193,8 @@ __global__ void __launch_bounds__(256) xcorr_rows_kernel(const float2* __restric
     const int W = 1 << logW;
     float2* tw = sm;
     float2* Ts = tw + (1 << (kTwLog - 1));         // [hw][kRowBlock]
-    float2* lines = Ts + hw * kRowBlock;           // [kRowBlock/2][W]
+    float2* lines = Ts + hw * kRowBlock;           // [kRowBlock/2][pad8(W)]
+    const int LW = pad8(W);
     const int f = blockIdx.y;
     const int y0 = blockIdx.x * kRowBlock;
     const float2* T = Gt + (long long)f * hw * H;
@@ -216,14 +219,14 @@ __global__ void __launch_bounds__(256) xcorr_rows_kernel(const float2* __restric
             else
                 z[h] = Ts[(W - k) * kRowBlock + r];
         }
-        lines[p * W + bitrev(k, logW)] = make_float2(z[0].x - z[1].y, z[0].y + z[1].x);
+        lines[p * LW + pad8(bitrev(k, logW))] = make_float2(z[0].x - z[1].y, z[0].y + z[1].x);
     }
     __syncthreads();
-    fft_stages(lines, logW, kRowBlock / 2, W, tw, kTwLog, +1);
+    fft_passes(lines, logW, kRowBlock / 2, LW, tw, kTwLog, +1);
     float* out = corr + (long long)f * W * H + (long long)y0 * W;
     for (int idx = threadIdx.x; idx < kRowBlock * W; idx += blockDim.x) {
         const int r = idx >> logW, x = idx & (W - 1);
-        const float2 v = lines[(r >> 1) * W + x];
+        const float2 v = lines[(r >> 1) * LW + pad8(x)];
         out[idx] = (r & 1) ? v.y : v.x;
     }
 }
@@ -264,7 +267,7 @@ cudaError_t launch_row_pass(int dtype, const void* frames, long long fstride, in
                             const dfc* twdf, cudaStream_t st)
 {
     const dim3 grid(g.H / kRowBlock, nframes);
-    const size_t smem = sizeof(dfc) * ((1 << (kTwLog - 1)) + (kRowBlock / 2) * g.W);
+    const size_t smem = sizeof(dfc) * ((1 << (kTwLog - 1)) + (kRowBlock / 2) * pad8(g.W));
     cudaError_t e = cudaSuccess;
     switch (dtype) {
     case 0:
@@ -294,8 +297,8 @@ cudaError_t launch_col_pass(int mode, const dfc* Gt, float2* S, const float2* Rb
 {
     const int nchunks = mode == 1 ? 1 : (nframes + fpc - 1) / fpc;
     const dim3 grid(g.hw, nchunks);
-    const size_t smem = sizeof(dfc) * ((1 << (kTwLog - 1)) + kColLines * g.H)
-                        + sizeof(float2) * ((1 << (kTwLog - 1)) + g.H + kColLines * g.H) + sizeof(double) * g.H;
+    const size_t smem = sizeof(dfc) * ((1 << (kTwLog - 1)) + kColLines * pad8(g.H))
+                        + sizeof(float2) * ((1 << (kTwLog - 1)) + g.H + kColLines * pad8(g.H)) + sizeof(double) * g.H;
     cudaError_t e = allow_smem(col_pass_kernel, smem);
     if (e != cudaSuccess)
         return e;
@@ -317,7 +320,7 @@ cudaError_t launch_xcorr_rows(const float2* T, float* corr, int nframes, const G
                               cudaStream_t st)
 {
     const dim3 grid(g.H / kRowBlock, nframes);
-    const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + g.hw * kRowBlock + (kRowBlock / 2) * g.W);
+    const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + g.hw * kRowBlock + (kRowBlock / 2) * pad8(g.W));
     cudaError_t e = allow_smem(xcorr_rows_kernel, smem);
     if (e != cudaSuccess)
         return e;

@@ -55,15 +55,16 @@ __device__ __forceinline__ bool unit_phasor(float2 b, float2* out)
     return true;
 }
 
-// float-float accumulation (Knuth two-sum; no multiplies, so no contraction)
+// float-float accumulation (Knuth two-sum).  The _rn intrinsics are never
+// contracted with a product the caller passes in.
 __device__ __forceinline__ void ff_add(float& hi, float& lo, float bh, float bl)
 {
-    const float s = hi + bh;
-    const float bb = s - hi;
-    float e = (hi - (s - bb)) + (bh - bb);
-    e += lo + bl;
-    hi = s + e;
-    lo = e - (hi - s);
+    const float s = __fadd_rn(hi, bh);
+    const float bb = __fsub_rn(s, hi);
+    float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+    e = __fadd_rn(e, __fadd_rn(lo, bl));
+    hi = __fadd_rn(s, e);
+    lo = __fsub_rn(e, __fsub_rn(hi, s));
 }
 
 // ----------------------------------------------------------------- plan

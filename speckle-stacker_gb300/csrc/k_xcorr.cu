@@ -12,6 +12,8 @@
 // to the lowest linear index (std::max_element's first maximum).  The bound
 // is 8 * 2^-24 * log2(W*H) * ||ref||_2 * ||frame||_2 * W*H, a few times the
 // worst-case error of an FP32 radix-2 FFT convolution.
+#include <cstdint>
+
 #include "smip_dev.cuh"
 
 namespace smip_gpu {
@@ -88,13 +90,38 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
     const int n = W * H;
     const float* c = corr + (long long)f * n;
     const T* fr = frames + (long long)f * fstride;
-    // ||frame||^2 and the FP32 peak
+    // ||frame||^2 and the FP32 peak.  corr rows are 16-byte aligned (n is a
+    // multiple of 256); the frame uses vector loads when its address allows.
     double sq = 0.0;
     float mx = -INFINITY;
-    for (int p = threadIdx.x; p < n; p += blockDim.x) {
-        const double v = (double)fr[p];
-        sq += v * v;
-        mx = fmaxf(mx, c[p]);
+    constexpr int PV = sizeof(T) == 8 ? 2 : 4;           // pixels per frame vector load
+    const bool vec = (reinterpret_cast<uintptr_t>(fr) & 15) == 0;
+    for (int p = threadIdx.x * 4; p < n; p += blockDim.x * 4) {
+        const float4 cv = *reinterpret_cast<const float4*>(c + p);
+        mx = fmaxf(fmaxf(mx, fmaxf(cv.x, cv.y)), fmaxf(cv.z, cv.w));
+        if (vec) {
+#pragma unroll
+            for (int q = 0; q < 4; q += PV) {
+                T px[PV];
+                if (sizeof(T) == 1)
+                    *reinterpret_cast<uint32_t*>(px) = *reinterpret_cast<const uint32_t*>(fr + p + q);
+                else if (sizeof(T) == 2)
+                    *reinterpret_cast<uint2*>(px) = *reinterpret_cast<const uint2*>(fr + p + q);
+                else
+                    *reinterpret_cast<uint4*>(px) = *reinterpret_cast<const uint4*>(fr + p + q);
+#pragma unroll
+                for (int e = 0; e < PV; ++e) {
+                    const double v = (double)px[e];
+                    sq += v * v;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const double v = (double)fr[p + e];
+                sq += v * v;
+            }
+        }
     }
     sq = block_sum(sq, redD);
 #pragma unroll
@@ -112,14 +139,7 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
 
     A best = 0;
     int best_idx = -1;
-    if (threadIdx.x == 0)
-        ncand = 0;
-    __syncthreads();
-    // Windows of blockDim.x positions; the candidate list is re-scored and
-    // emptied whenever the next window would overflow it, so every position
-    // with c >= thr is re-scored exactly once.
-    auto flush = [&]() {
-        const int nc = ncand;
+    auto rescore = [&](int nc) {
         for (int q = 0; q < nc; ++q) {
             const int p = cand[q];
             const A v = exact_corr(ref, fr, W, H, p & (W - 1), p / W, redA);
@@ -128,24 +148,56 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
                 best_idx = p;
             }
         }
-        __syncthreads();
+    };
+    // One pass collects every position with c >= thr (the winner is chosen by
+    // exact value, then lowest index, so collection order does not matter).
+    if (threadIdx.x == 0)
+        ncand = 0;
+    __syncthreads();
+    for (int p = threadIdx.x * 4; p < n; p += blockDim.x * 4) {
+        const float4 cv = *reinterpret_cast<const float4*>(c + p);
+        const float e4[4] = { cv.x, cv.y, cv.z, cv.w };
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+            if (e4[e] >= thr) {
+                const int slot = atomicAdd(&ncand, 1);
+                if (slot < kMaxCand)
+                    cand[slot] = p + e;
+            }
+    }
+    __syncthreads();
+    const int total_cand = ncand;
+    __syncthreads();
+    if (total_cand <= kMaxCand) {
+        rescore(total_cand);
+    } else {
+        // More candidates than the list holds: windows of blockDim.x
+        // positions, the list re-scored and emptied whenever the next window
+        // would overflow it, so every position with c >= thr is re-scored once.
         if (threadIdx.x == 0)
             ncand = 0;
         __syncthreads();
-    };
-    for (int base = 0; base < n; base += blockDim.x) {
-        const int p = base + threadIdx.x;
-        const bool hit = p < n && c[p] >= thr;
-        const int wc = __syncthreads_count(hit);
-        if (wc == 0)
-            continue;
-        if (ncand + wc > kMaxCand)
-            flush();
-        if (hit)
-            cand[atomicAdd(&ncand, 1)] = p;
-        __syncthreads();
+        auto flush = [&]() {
+            rescore(ncand);
+            __syncthreads();
+            if (threadIdx.x == 0)
+                ncand = 0;
+            __syncthreads();
+        };
+        for (int base = 0; base < n; base += blockDim.x) {
+            const int p = base + threadIdx.x;
+            const bool hit = p < n && c[p] >= thr;
+            const int wc = __syncthreads_count(hit);
+            if (wc == 0)
+                continue;
+            if (ncand + wc > kMaxCand)
+                flush();
+            if (hit)
+                cand[atomicAdd(&ncand, 1)] = p;
+            __syncthreads();
+        }
+        flush();
     }
-    flush();
     if (threadIdx.x == 0) {
         int sx = best_idx & (W - 1), sy = best_idx / W;
         sx -= (sx < (W + 1) / 2) ? 0 : W;
@@ -162,15 +214,35 @@ __device__ __forceinline__ double abs_px(double v) { return fabs(v); }
 // order (main.cpp:293-294); the stack's frame 0 enters unshifted with its
 // sign (main.cpp:266).
 template <typename T, typename A>
-__global__ void saa_add_kernel(A* __restrict__ sum, const T* __restrict__ frames, long long fstride, int nframes,
-                               int first_is_frame0, const int* __restrict__ shifts, int W, int H)
+__global__ void __launch_bounds__(256) saa_add_kernel(A* __restrict__ sum, const T* __restrict__ frames,
+                                                      long long fstride, int nframes, int first_is_frame0,
+                                                      const int* __restrict__ shifts, int W, int H)
 {
+    extern __shared__ int2 sh[]; // the batch's shifts
+    for (int f = threadIdx.x; f < nframes; f += blockDim.x)
+        sh[f] = make_int2(shifts[2 * f], shifts[2 * f + 1]);
+    __syncthreads();
     const int n = W * H;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const int x = p & (W - 1), y = p / W;
         A acc = sum[p];
-        for (int f = 0; f < nframes; ++f) {
-            const int xs = x + shifts[2 * f], ys = y + shifts[2 * f + 1];
+        int f = 0;
+        for (; f + 8 <= nframes; f += 8) { // eight independent loads in flight, added in frame order
+            A v[8];
+            bool in[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int xs = x + sh[f + q].x, ys = y + sh[f + q].y;
+                in[q] = xs >= 0 && xs < W && ys >= 0 && ys < H;
+                v[q] = in[q] ? (A)frames[(long long)(f + q) * fstride + ys * W + xs] : (A)0;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (in[q])
+                    acc += (first_is_frame0 && f + q == 0) ? v[q] : abs_px(v[q]);
+        }
+        for (; f < nframes; ++f) {
+            const int xs = x + sh[f].x, ys = y + sh[f].y;
             if (xs >= 0 && xs < W && ys >= 0 && ys < H) {
                 const A v = (A)frames[(long long)f * fstride + ys * W + xs];
                 acc += (first_is_frame0 && f == 0) ? v : abs_px(v);
@@ -212,11 +284,12 @@ cudaError_t launch_saa_add(int dtype, void* sum, const void* frames, long long f
 {
     const int n = g.W * g.H;
     const int grid = (n + 255) / 256;
+    const size_t shm = sizeof(int2) * (size_t)(nframes > 0 ? nframes : 1);
     switch (dtype) {
-    case 0: saa_add_kernel<uint8_t, unsigned long long><<<grid, 256, 0, st>>>((unsigned long long*)sum, (const uint8_t*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
-    case 1: saa_add_kernel<uint16_t, unsigned long long><<<grid, 256, 0, st>>>((unsigned long long*)sum, (const uint16_t*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
-    case 2: saa_add_kernel<float, double><<<grid, 256, 0, st>>>((double*)sum, (const float*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
-    default: saa_add_kernel<double, double><<<grid, 256, 0, st>>>((double*)sum, (const double*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
+    case 0: saa_add_kernel<uint8_t, unsigned long long><<<grid, 256, shm, st>>>((unsigned long long*)sum, (const uint8_t*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
+    case 1: saa_add_kernel<uint16_t, unsigned long long><<<grid, 256, shm, st>>>((unsigned long long*)sum, (const uint16_t*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
+    case 2: saa_add_kernel<float, double><<<grid, 256, shm, st>>>((double*)sum, (const float*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
+    default: saa_add_kernel<double, double><<<grid, 256, shm, st>>>((double*)sum, (const double*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
     }
     return cudaGetLastError();
 }

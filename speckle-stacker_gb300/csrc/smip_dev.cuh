@@ -65,29 +65,32 @@ __device__ void fft_stages(C* buf, int logn, int nl, int ls, const C* tw, int tw
 // drop only the lo*lo term.  Used for the forward frame FFT so that weak
 // frequency bins keep full FP32 relative accuracy after rounding, as an FP64
 // transform narrowed to FP32 would give them.
+// The error-free steps use __fadd_rn / __fsub_rn / __fmul_rn, which the
+// compiler never contracts into an FMA with a neighbouring product (a
+// contracted p + e would silently drop the low word).
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
 {
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
 __device__ __forceinline__ void df_add(float ah, float al, float bh, float bl, float& rh, float& rl)
 {
     float s, e;
     two_sum(ah, bh, s, e);
-    e += al + bl;
-    rh = s + e;
-    rl = e - (rh - s);
+    e = __fadd_rn(e, __fadd_rn(al, bl));
+    rh = __fadd_rn(s, e);
+    rl = __fsub_rn(e, __fsub_rn(rh, s));
 }
 
 __device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, float& rh, float& rl)
 {
-    const float p = ah * bh;
+    const float p = __fmul_rn(ah, bh);
     float e = fmaf(ah, bh, -p);
     e = fmaf(ah, bl, fmaf(al, bh, e));
-    rh = p + e;
-    rl = e - (rh - p);
+    rh = __fadd_rn(p, e);
+    rl = __fsub_rn(e, __fsub_rn(rh, p));
 }
 
 __device__ __forceinline__ dfc df_cadd(const dfc& a, const dfc& b)
@@ -144,6 +147,97 @@ __device__ inline void df_fft_stages(dfc* buf, int logn, int nl, int ls, const d
             L[i0 + half] = df_csub(a, t);
         }
         __syncthreads();
+    }
+}
+
+// ------------------------------------------ register-staged radix-2 passes
+// Same transform, twiddles and per-butterfly arithmetic as fft_stages /
+// df_fft_stages (so results are bit-identical), but a thread loads the 2^K
+// elements that K consecutive stages combine, runs those stages in registers
+// and stores once: one shared-memory round trip and one __syncthreads per
+// pass of up to 3 stages instead of per stage.  Lines are stored padded, one
+// spare element per 8 (element e of a line at pad8(e), line length pad8(n)),
+// which keeps the strided accesses of the first pass free of bank conflicts.
+__device__ __host__ __forceinline__ int pad8(int e) { return e + (e >> 3); }
+
+__device__ __forceinline__ void bfly(float2& a, float2& b, float2 w)
+{
+    const float2 t = cmul(b, w);
+    const float2 u = a;
+    a = cadd(u, t);
+    b = csub(u, t);
+}
+__device__ __forceinline__ void bfly(dfc& a, dfc& b, const dfc& w)
+{
+    const dfc t = df_cmul(b, w);
+    const dfc u = a;
+    a = df_cadd(u, t);
+    b = df_csub(u, t);
+}
+__device__ __forceinline__ float2 tw_conj(float2 w)
+{
+    w.y = -w.y;
+    return w;
+}
+__device__ __forceinline__ dfc tw_conj(dfc w)
+{
+    w.h.y = -w.h.y;
+    w.l.y = -w.l.y;
+    return w;
+}
+
+// Stages s0+1 .. s0+K of an n = 2^logn DIT FFT on nl padded lines (stride ls).
+template <int K, typename C>
+__device__ __forceinline__ void fft_pass(C* buf, int logn, int nl, int ls, const C* tw, int twlog, int sign, int s0)
+{
+    const int gsh = logn - K; // log2 of the groups per line
+    const int ng = nl << gsh;
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+        const int line = g >> gsh, q = g & ((1 << gsh) - 1);
+        const int j = q & ((1 << s0) - 1);
+        const int base = ((q >> s0) << (s0 + K)) + j;
+        C* L = buf + line * ls;
+        C v[1 << K];
+#pragma unroll
+        for (int m = 0; m < (1 << K); ++m)
+            v[m] = L[pad8(base + (m << s0))];
+#pragma unroll
+        for (int t = 1; t <= K; ++t) {
+            const int hm = 1 << (t - 1);
+            const int tsh = twlog - (s0 + t);
+#pragma unroll
+            for (int m0 = 0; m0 < (1 << K); ++m0) {
+                if (m0 & hm)
+                    continue;
+                C w = tw[(((m0 & (hm - 1)) << s0) + j) << tsh];
+                if (sign > 0)
+                    w = tw_conj(w);
+                bfly(v[m0], v[m0 + hm], w);
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < (1 << K); ++m)
+            L[pad8(base + (m << s0))] = v[m];
+    }
+    __syncthreads();
+}
+
+// In-place DIT FFT of nl padded lines of length n = 2^logn (logn >= 3), input in
+// bit-reversed order, in passes of at most 3 stages.  Called by all threads.
+template <typename C>
+__device__ void fft_passes(C* buf, int logn, int nl, int ls, const C* tw, int twlog, int sign)
+{
+    const int np = (logn + 2) / 3;
+    int s0 = 0;
+    for (int p = 0; p < np; ++p) {
+        const int k = (logn - s0 + (np - p) - 1) / (np - p);
+        if (k == 3)
+            fft_pass<3>(buf, logn, nl, ls, tw, twlog, sign, s0);
+        else if (k == 2)
+            fft_pass<2>(buf, logn, nl, ls, tw, twlog, sign, s0);
+        else
+            fft_pass<1>(buf, logn, nl, ls, tw, twlog, sign, s0);
+        s0 += k;
     }
 }
 

@@ -17,7 +17,7 @@ enum : int {
 constexpr int kMaxLog = 9;        // frames up to 512 x 512
 constexpr int kTwLog = kMaxLog;   // twiddle table for length 2^kTwLog
 constexpr int kRowBlock = 16;     // rows per CTA in the row passes
-constexpr int kColLines = 4;      // frames per FFT pass in the column kernel
+constexpr int kColLines = 8;      // frames per FFT pass in the column kernel
 
 // Geometry of one stack (all derived from ncols = W, nrows = H, depth).
 struct Geometry {

@@ -133,6 +133,20 @@ def test_xcorr_gaussian_fixture(smip, oracle):
     assert smip.CrossCorrelation(g).get_displacement(g, oracle.shifted(g, 3, -4)) == (3, -4)
 
 
+def test_repeat_runs_bit_identical(smip):
+    """The same frames give bit-identical results run after run: every output
+    of the per-frame pipeline and the phase map.  Catches races between the
+    bispectrum kernel's shared-memory ring and its TMA refills."""
+    from smip_gb300 import synthetic as S
+
+    spec = S.config_spec("extended256", nframes=24)
+    frames = S.make_stack(spec)
+    runs = [run_gpu(smip, frames, spec.bdepth, spec.reco_radius, batch=8) for _ in range(3)]
+    for r in runs[1:]:
+        for key in ("shifts", "sum", "power", "bispec", "phases", "image"):
+            assert np.array_equal(np.asarray(r[key]), np.asarray(runs[0][key])), key
+
+
 def test_merge_equals_single_stack(smip):
     from smip_gb300 import synthetic as S
 
