@@ -52,18 +52,77 @@ template <> __device__ __forceinline__ unsigned long long mul_exact<unsigned lon
     return (unsigned long long)((unsigned)a * (unsigned)b);
 }
 
+constexpr int kMulti = 8; // candidates scored per sweep over the frame
+
+// Exact correlations sum_p ref(p) frame((p + s_c) mod (W, H)) of up to kMulti
+// candidate shifts s_c = cand[c] (row-major index) in one sweep: four
+// consecutive pixels per thread step, shifts and masks instead of divisions.
+// Results land in out[c] for every thread.
 template <typename T>
-__device__ typename ExactAcc<T>::type exact_corr(const T* ref, const T* fr, int W, int H, int sx, int sy,
-                                                 typename ExactAcc<T>::type* red)
+__device__ void exact_corr_multi(const T* __restrict__ ref, const T* __restrict__ fr, int logW, int H,
+                                 const int* cand, int k, typename ExactAcc<T>::type* out,
+                                 typename ExactAcc<T>::type* red /* [kMulti][32] */)
 {
     using A = typename ExactAcc<T>::type;
-    A acc = 0;
-    for (int p = threadIdx.x; p < W * H; p += blockDim.x) {
-        const int x = p & (W - 1), y = p / W;
-        const int xs = (x + sx) & (W - 1), ys = (y + sy) & (H - 1);
-        acc += mul_exact<A>(ref[p], fr[ys * W + xs]);
+    const int W = 1 << logW, n = W * H;
+    A acc[kMulti];
+#pragma unroll
+    for (int c = 0; c < kMulti; ++c)
+        acc[c] = 0;
+    int sx[kMulti], sy[kMulti];
+#pragma unroll
+    for (int c = 0; c < kMulti; ++c) {
+        const int q = c < k ? cand[c] : 0;
+        sx[c] = q & (W - 1);
+        sy[c] = q >> logW;
     }
-    return block_sum(acc, red);
+    const bool vec = (reinterpret_cast<uintptr_t>(ref) & 15) == 0;
+    for (int p = threadIdx.x * 4; p < n; p += blockDim.x * 4) {
+        const int x = p & (W - 1), y = p >> logW;
+        T r4[4];
+        if (vec && sizeof(T) == 1)
+            *reinterpret_cast<uint32_t*>(r4) = *reinterpret_cast<const uint32_t*>(ref + p);
+        else if (vec && sizeof(T) == 2)
+            *reinterpret_cast<uint2*>(r4) = *reinterpret_cast<const uint2*>(ref + p);
+        else if (vec && sizeof(T) == 4)
+            *reinterpret_cast<uint4*>(r4) = *reinterpret_cast<const uint4*>(ref + p);
+        else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                r4[e] = ref[p + e];
+        }
+#pragma unroll
+        for (int c = 0; c < kMulti; ++c) {
+            if (c < k) {
+                const T* row = fr + (((y + sy[c]) & (H - 1)) << logW);
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    acc[c] += mul_exact<A>(r4[e], row[(x + e + sx[c]) & (W - 1)]);
+            }
+        }
+    }
+    // block reduction of the k sums at once
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int c = 0; c < kMulti; ++c) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+    }
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < kMulti; ++c)
+            red[c * 32 + w] = acc[c];
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < kMulti; ++c) {
+        A t = 0;
+        for (int i = 0; i < nw; ++i)
+            t += red[c * 32 + i];
+        out[c] = t;
+    }
+    __syncthreads();
 }
 
 template <typename T>
@@ -74,8 +133,8 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
                                                                      int* __restrict__ shifts)
 {
     using A = typename ExactAcc<T>::type;
-    __shared__ A redA[32];
-    __shared__ double redD[32];
+    __shared__ A redM[kMulti * 32];
+    __shared__ A redA1[32];
     __shared__ float redF[32];
     __shared__ int cand[kMaxCand];
     __shared__ int ncand;
@@ -92,7 +151,7 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
     const T* fr = frames + (long long)f * fstride;
     // ||frame||^2 and the FP32 peak.  corr rows are 16-byte aligned (n is a
     // multiple of 256); the frame uses vector loads when its address allows.
-    double sq = 0.0;
+    A sqa = 0; // exact (u64) for integer frames, FP64 for float frames
     float mx = -INFINITY;
     constexpr int PV = sizeof(T) == 8 ? 2 : 4;           // pixels per frame vector load
     const bool vec = (reinterpret_cast<uintptr_t>(fr) & 15) == 0;
@@ -110,20 +169,16 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
                 else
                     *reinterpret_cast<uint4*>(px) = *reinterpret_cast<const uint4*>(fr + p + q);
 #pragma unroll
-                for (int e = 0; e < PV; ++e) {
-                    const double v = (double)px[e];
-                    sq += v * v;
-                }
+                for (int e = 0; e < PV; ++e)
+                    sqa += mul_exact<A>(px[e], px[e]);
             }
         } else {
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const double v = (double)fr[p + e];
-                sq += v * v;
-            }
+            for (int e = 0; e < 4; ++e)
+                sqa += mul_exact<A>(fr[p + e], fr[p + e]);
         }
     }
-    sq = block_sum(sq, redD);
+    const double sq = (double)block_sum(sqa, redA1);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
         mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -140,12 +195,16 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
     A best = 0;
     int best_idx = -1;
     auto rescore = [&](int nc) {
-        for (int q = 0; q < nc; ++q) {
-            const int p = cand[q];
-            const A v = exact_corr(ref, fr, W, H, p & (W - 1), p / W, redA);
-            if (best_idx < 0 || v > best || (v == best && p < best_idx)) {
-                best = v;
-                best_idx = p;
+        for (int q0 = 0; q0 < nc; q0 += kMulti) {
+            const int k = nc - q0 < kMulti ? nc - q0 : kMulti;
+            A v[kMulti];
+            exact_corr_multi(ref, fr, __ffs(W) - 1, H, cand + q0, k, v, redM);
+            for (int c = 0; c < k; ++c) {
+                const int p = cand[q0 + c];
+                if (best_idx < 0 || v[c] > best || (v[c] == best && p < best_idx)) {
+                    best = v[c];
+                    best_idx = p;
+                }
             }
         }
     };
