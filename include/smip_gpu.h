@@ -6,8 +6,8 @@
  * shift-and-add, closure-phase recovery, final reconstruction).  All entry
  * points are extern "C", take plain pointers and sizes, return an int status
  * (SMIP_OK = 0) and leave a thread-local message for smip_last_error().
- * The C++ layer in speckle-stacker_gb300/include/smip/ maps the status codes
- * back to the exception types the reference throws.
+ * The C++ layer in speckle-stacker_gb300/include/smip/gpu.hpp maps the status
+ * codes back to the exception types the reference throws.
  *
  * Conventions (the reference's own):
  *   - 2-D arrays are ncols x nrows, row-major, x fastest; spectra, phases and
@@ -75,8 +75,8 @@ SMIP_GPU_API int smip_version(int* major, int* minor, int* patch);
  * (bispectrum.h:183-192, main.cpp:253) plus the accumulators above.
  * stream: a cudaStream_t to run on, or NULL for a stream owned by the stack.
  * batch_frames: frames per accumulation batch (0 = library default).
- * Supported: ncols, nrows powers of two in [16, 1024]; bdepth/2*2 a multiple
- * of 8 in [8, 64] and < min(ncols, nrows). */
+ * Supported: ncols, nrows powers of two in [16, 512]; bdepth/2*2 in [2, 64]
+ * and < min(ncols, nrows). */
 SMIP_GPU_API int smip_stack_create(smip_stack_t* out, int device, long ncols, long nrows,
                                    long bdepth, void* stream, long batch_frames);
 SMIP_GPU_API int smip_stack_destroy(smip_stack_t s);
@@ -149,9 +149,17 @@ SMIP_GPU_API int smip_stack_merge(smip_stack_t dst, smip_stack_t src);
 /* Makes src correlate against dst's reference frame (frame 0 of dst). */
 SMIP_GPU_API int smip_stack_share_reference(smip_stack_t dst, smip_stack_t src);
 
-/* Bispectrum::write_to_file / read_from_file (bispectrum.h:411-462): the
- * normalised bispectrum in the reference's bispectrum.dat format. */
+/* Bispectrum::write_to_file (bispectrum.h:411-430): the normalised
+ * bispectrum in the reference's bispectrum.dat format. */
 SMIP_GPU_API int smip_stack_save_bispectrum(smip_stack_t s, const char* path);
+
+/* Bispectrum::read_from_file (bispectrum.h:432-462) into an empty stack of the
+ * same shape: the accumulator resumes as the file's (normalised) bispectrum
+ * times nframes (0 = 1) with zero compensation, so smip_stack_reconstruct runs
+ * on it and smip_stack_accumulate_fft can add further spectra (a stack needs
+ * its reference frame for frames, so smip_stack_push_frames is refused).
+ * SMIP_E_RUNTIME on I/O errors, SMIP_E_INVALID_ARGUMENT on a shape mismatch. */
+SMIP_GPU_API int smip_stack_load_bispectrum(smip_stack_t s, const char* path, long nframes);
 
 /* ========================================================================== *
  * Standalone calls mirroring the reference's free functions and classes.

@@ -62,7 +62,6 @@ struct BCfg {
     static constexpr int NJB = WARPS / (RPC * NLB);        // 32-wide j blocks per tile
     static constexpr int JT = 32 * NJB;                    // tile j width
     static constexpr int THREADS = WARPS * 32;
-    static constexpr int NCHM = ROWS / RPC;                // main chunks per (a0, j tile)
     static constexpr int NWV = 8 + 2 * (TLW - 1);          // W values per thread per frame
     static constexpr int BW = JT + DE + 2;                 // W box columns (even start)
     static constexpr int BV = DE + 2;                      // V box columns (even start)
@@ -86,6 +85,8 @@ struct BispecArgs {
     int* err;
     int nframes;
     int H, hw;
+    int D;        // the stack's depth (even, <= DE): packed layout and stored elements
+    int nchm;     // main chunks per (a0, j tile): ceil((D/2) / RPC)
     int njt;      // j tiles: ceil(H / JT)
     int nmain;    // main tiles
     int ntiles;   // main + row-0 tiles
@@ -107,8 +108,8 @@ __device__ __forceinline__ TileInfo decode_tile(int t, const BispecArgs& p)
     ti.row0 = t >= p.nmain;
     int jt;
     if (!ti.row0) {
-        ti.c = t % Cf::NCHM;
-        const int rest = t / Cf::NCHM;
+        ti.c = t % p.nchm;
+        const int rest = t / p.nchm;
         jt = rest % p.njt;
         ti.a0 = rest / p.njt;
     } else {
@@ -281,17 +282,18 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
         }
         if (!ok)
             break;
-        if (a0 < p.hw && jw < half_h) {
+        const int hd = p.D / 2; // a depth below DE computes the template's extra rows and columns, stores none
+        if (a0 < p.hw && jw < half_h && a2 <= hd) {
             // Kahan-compensated add of the batch partial into (B, C); within a
             // j step every load is issued before the first store (B and C never
             // alias).
             const int H = p.H;
-            constexpr int rowE = (DE / 2 + 1) * (DE + 1);
-            float2* __restrict__ Bt = p.B + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (DE + 1);
-            float2* __restrict__ Ct = p.C + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (DE + 1);
+            const int rowE = (hd + 1) * (p.D + 1);
+            float2* __restrict__ Bt = p.B + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (p.D + 1);
+            float2* __restrict__ Ct = p.C + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (p.D + 1);
             auto off = [&](int j, int l) {
                 const int a1 = j >= 0 ? j : j + H + 1;
-                const int a3 = l >= 0 ? l : l + DE + 1;
+                const int a3 = l >= 0 ? l : l + p.D + 1;
                 return a1 * rowE + a3;
             };
             auto kahan = [](float2& b, float2& c, float2 v) {
@@ -302,7 +304,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
                 b = make_float2(tx, ty);
             };
             // a tile may reach past j = H/2 - 1 when H < JT: those sums are zero and not stored
-            const bool has_e = edge && jw + lane < half_h;
+            const bool has_e = edge && jw + lane < half_h && DE == p.D;
             const int oe = off(jw + lane, DE / 2);
             float2 be = make_float2(0.f, 0.f), ce = be;
             if (has_e) {
@@ -315,16 +317,20 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
                 if (j < half_h) {
                     int o[Cf::TLW];
                     float2 bv[Cf::TLW], cvv[Cf::TLW];
+                    bool st[Cf::TLW];
 #pragma unroll
-                    for (int b = 0; b < Cf::TLW; ++b)
-                        if (b < nb) {
-                            o[b] = off(j, -DE / 2 + 8 * Cf::TLW * lb + lg + 8 * b);
+                    for (int b = 0; b < Cf::TLW; ++b) {
+                        const int l = -DE / 2 + 8 * Cf::TLW * lb + lg + 8 * b;
+                        st[b] = b < nb && l >= -hd && l <= hd;
+                        if (st[b]) {
+                            o[b] = off(j, l);
                             bv[b] = Bt[o[b]];
                             cvv[b] = Ct[o[b]];
                         }
+                    }
 #pragma unroll
                     for (int b = 0; b < Cf::TLW; ++b)
-                        if (b < nb) {
+                        if (st[b]) {
                             kahan(bv[b], cvv[b], acc[a][b]);
                             Bt[o[b]] = bv[b];
                             Ct[o[b]] = cvv[b];
@@ -404,21 +410,25 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
     a.nframes = L.nframes;
     a.H = g.H;
     a.hw = g.hw;
+    a.D = g.De;
+    a.nchm = (g.De / 2 + Cf::RPC - 1) / Cf::RPC;
     a.njt = (g.H + Cf::JT - 1) / Cf::JT;
-    a.nmain = g.hw * a.njt * Cf::NCHM;
+    a.nmain = g.hw * a.njt * a.nchm;
     a.ntiles = a.nmain + (g.hw + Cf::RPC - 1) / Cf::RPC * a.njt;
     const int grid = a.ntiles < L.num_sms ? a.ntiles : L.num_sms;
     bispec_accum_kernel<DE><<<grid, Cf::THREADS, Cf::SMEM, st>>>(mW, mV, mA, a); note_launches(1);
     return cudaGetLastError();
 }
 
-bool bispec_depth_supported(int De) { return De >= 8 && De <= 64 && De % 8 == 0; }
+bool bispec_depth_supported(int De) { return De >= 2 && De <= 64 && De % 2 == 0; }
 
+// The kernel is instantiated for depths that are multiples of 8; another even
+// depth runs the next one up and stores only its own elements.
 cudaError_t launch_bispec_accumulate(const BispecLaunch& L, const Geometry& g, cudaStream_t st)
 {
     if (L.nframes <= 0)
         return cudaSuccess;
-    switch (g.De) {
+    switch ((g.De + 7) / 8 * 8) {
     case 8: return launch_de<8>(L, g, st);
     case 16: return launch_de<16>(L, g, st);
     case 24: return launch_de<24>(L, g, st);

@@ -138,7 +138,7 @@ int make_geometry(long W, long H, long bdepth, Geometry* g)
     if (bdepth < 0)
         return fail(SMIP_E_INVALID_ARGUMENT, "bdepth must be non-negative");
     if (!bispec_depth_supported(De))
-        return fail(SMIP_E_UNSUPPORTED, "bispectrum depth (rounded down to even) must be a multiple of 8 in [8, 64]");
+        return fail(SMIP_E_UNSUPPORTED, "bispectrum depth (rounded down to even) must be in [2, 64]");
     if (De >= W || De >= H)
         return fail(SMIP_E_UNSUPPORTED, "bispectrum depth must be smaller than the frame size");
     g->W = (int)W;
@@ -913,6 +913,50 @@ extern "C" int smip_stack_save_bispectrum(smip_stack_t s, const char* path)
     std::fclose(f);
     if (!ok)
         return fail(SMIP_E_RUNTIME, std::string("error writing ") + path);
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_load_bispectrum(smip_stack_t s, const char* path, long nframes)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    if (!path)
+        return fail(SMIP_E_INVALID_ARGUMENT, "null path");
+    if (s->nframes != 0)
+        return fail(SMIP_E_INVALID_ARGUMENT, "stack already holds frames; reset it before loading a bispectrum");
+    FILE* f = std::fopen(path, "rb");
+    if (!f)
+        return fail(SMIP_E_RUNTIME, std::string("unable to open file ") + path);
+    // bispectrum.h:442-461: size_t base_size, 4 x size_t dims, T[base_size]
+    size_t hdr[5] = { 0, 0, 0, 0, 0 };
+    if (std::fread(hdr, sizeof(size_t), 5, f) != 5) {
+        std::fclose(f);
+        return fail(SMIP_E_RUNTIME, std::string("error reading bispectrum metadata from file ") + path);
+    }
+    if (hdr[0] != (size_t)s->g.base_size || hdr[1] != (size_t)s->g.W || hdr[2] != (size_t)s->g.H
+        || hdr[3] / 2 * 2 != (size_t)s->g.De || hdr[4] / 2 * 2 != (size_t)s->g.De) {
+        std::fclose(f);
+        return fail(SMIP_E_INVALID_ARGUMENT, std::string("bispectrum file ") + path + " has another shape than the stack");
+    }
+    const size_t n = hdr[0];
+    std::vector<float> buf(2 * n);
+    const bool ok = std::fread(buf.data(), sizeof(float) * 2, n, f) == n;
+    std::fclose(f);
+    if (!ok)
+        return fail(SMIP_E_RUNTIME, std::string("error reading data block from file ") + path);
+    // the file holds the normalised bispectrum: the accumulator resumes as
+    // file x nframes with zero compensation, over nframes frames
+    const long nf = nframes > 0 ? nframes : 1;
+    if (nf != 1)
+        for (float& v : buf)
+            v = (float)((double)v * (double)nf);
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    CUDA_TRY(cudaMemcpy(s->B, buf.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemset(s->C, 0, sizeof(float2) * n));
+    s->nframes = nf;
+    s->pending = 0;
+    s->mode = 2; // spectra may be added (accumulate_fft); frames need their reference frame
     return SMIP_OK;
 }
 

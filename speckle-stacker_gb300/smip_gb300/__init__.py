@@ -105,6 +105,7 @@ def _load():
         "smip_stack_merge": ([vp, vp], C.c_int),
         "smip_stack_share_reference": ([vp, vp], C.c_int),
         "smip_stack_save_bispectrum": ([vp, C.c_char_p], C.c_int),
+        "smip_stack_load_bispectrum": ([vp, C.c_char_p, C.c_long], C.c_int),
         "smip_reconstruct_phases": ([C.c_int, fp, C.c_long, C.c_long, C.c_long, C.c_double, dp, ubp, dp], C.c_int),
         "smip_next_reco_index": ([dp, dp, ip, ip], C.c_int),
         "smip_reco_visits": ([C.c_double, ip, C.c_long, lp], C.c_int),
@@ -310,6 +311,12 @@ class Stack:
 
     def save_bispectrum(self, path: str):
         _check(_L().smip_stack_save_bispectrum(self._h, path.encode()))
+
+    def load_bispectrum(self, path: str, nframes: int = 0):
+        """Bispectrum::read_from_file (bispectrum.h:432-462) into this empty
+        stack: the accumulator resumes as the file's normalised bispectrum x
+        nframes (0 = 1); reconstruct_phases and accumulate_from_fft work on it."""
+        _check(_L().smip_stack_load_bispectrum(self._h, path.encode(), int(nframes)))
 
 
 # ------------------------------------------------------- free functions

@@ -37,7 +37,8 @@ def test_next_reco_index_and_visits(smip):
         assert hashlib.sha256(v.astype(np.int32).tobytes()).hexdigest() == str(fx[f"r{R}_sha"])
 
 
-@pytest.mark.parametrize("shape", [(100, 128, 16), (128, 128, 12), (128, 128, 128), (8, 8, 4), (1024, 1024, 16)])
+@pytest.mark.parametrize("shape", [(100, 128, 16), (128, 128, 66), (128, 128, 1), (128, 128, 128), (8, 8, 4),
+                                   (1024, 1024, 16), (16, 16, 16)])
 def test_unsupported_shapes_rejected(smip, shape):
     with pytest.raises(smip.Unsupported):
         smip.Stack(*shape)

@@ -1,0 +1,155 @@
+"""smip-cli (speckle-stacker_gb300/cli/smip_cli.cpp) and the C++ layer
+(speckle-stacker_gb300/include/smip/gpu.hpp): the reference's command line and
+C++ call pattern over the C ABI.
+
+CPU tests check the command line without a device and that a C++ program
+builds against the header layer; GPU tests run both and compare every output
+with the ctypes binding, which the parity tests check against the oracle."""
+import os
+import shutil
+import struct
+import subprocess
+import zlib
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG = os.path.join(ROOT, "speckle-stacker_gb300")
+CLI = os.path.join(PKG, "bin", "smip-cli")
+
+
+def _need_cli():
+    if not os.path.exists(CLI):
+        pytest.skip("smip-cli not built (make -C speckle-stacker_gb300)")
+
+
+def read_png16(path):
+    """Minimal reader for the CLI's 16-bit gray/RGB PNGs (stored or deflated)."""
+    data = open(path, "rb").read()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, idat, ihdr = 8, b"", None
+    while pos < len(data):
+        n, typ = struct.unpack(">I4s", data[pos:pos + 8])
+        body = data[pos + 8:pos + 8 + n]
+        assert struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])[0] == zlib.crc32(typ + body)
+        if typ == b"IHDR":
+            ihdr = struct.unpack(">IIBBBBB", body)
+        elif typ == b"IDAT":
+            idat += body
+        pos += 12 + n
+    w, h, depth, ctype = ihdr[:4]
+    assert depth == 16 and ctype in (0, 2)
+    ch = 3 if ctype == 2 else 1
+    raw = zlib.decompress(idat)
+    rows = np.frombuffer(raw, np.uint8).reshape(h, 1 + w * ch * 2)
+    assert np.all(rows[:, 0] == 0)
+    return rows[:, 1:].copy().view(">u2").astype(np.uint16).reshape(h, w, ch)[..., 0 if ch == 1 else slice(None)]
+
+
+def test_cli_version_and_help():
+    _need_cli()
+    out = subprocess.run([CLI, "--version"], capture_output=True, text=True, check=True)
+    assert "v0.3.2" in out.stdout
+    out = subprocess.run([CLI, "-h"], capture_output=True, text=True, check=True)
+    for flag in ("--nrframes", "--refframe", "--recoradius", "--bdepth", "--channel", "--croppos", "--cropsize",
+                 "--no-calcsum", "--no-specklemasking", "--verbose", "--version"):
+        assert flag in out.stdout
+    # no source: usage, exit 0 (main.cpp:215-218)
+    assert subprocess.run([CLI], capture_output=True).returncode == 0
+
+
+def test_cli_rejects_bad_input(tmp_path):
+    _need_cli()
+    bad = tmp_path / "x.npy"
+    np.save(bad, np.zeros((2, 16, 16), np.int32))
+    r = subprocess.run([CLI, str(bad)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 1 and "unsupported dtype" in r.stderr
+    r = subprocess.run([CLI, str(tmp_path / "missing.npy")], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 1 and "file open error" in r.stderr
+    r = subprocess.run([CLI, "-k", "-1:3", str(bad)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 1 and "crop box" in r.stderr
+
+
+def _build_api_check(out_dir):
+    exe = os.path.join(out_dir, "api_check")
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I" + os.path.join(ROOT, "include"),
+           "-I" + os.path.join(PKG, "include"), os.path.join(ROOT, "tests", "cpp", "api_check.cpp"),
+           "-L" + os.path.join(PKG, "lib"), "-lsmip_gpu", "-Wl,-rpath," + os.path.join(PKG, "lib"), "-o", exe]
+    subprocess.run(cmd, check=True)
+    return exe
+
+
+def test_cpp_layer_builds(tmp_path):
+    if shutil.which("g++") is None or not os.path.exists(os.path.join(PKG, "lib", "libsmip_gpu.so")):
+        pytest.skip("g++ or libsmip_gpu.so missing")
+    assert os.path.exists(_build_api_check(str(tmp_path)))
+
+
+@pytest.mark.gpu
+def test_cli_matches_binding(smip, tmp_path):
+    """smip-cli -b 20 -p 40 -n 10 on a 12-frame u8 stack: bispectrum.dat and every
+    PNG equal what the binding gives for the same frames (default depth 20)."""
+    _need_cli()
+    from smip_gb300 import synthetic as S
+
+    frames = S.make_stack(S.config_spec("binary128", nframes=12))
+    src = tmp_path / "stack.npy"
+    np.save(src, frames)
+    r = subprocess.run([CLI, "-b", "20", "-p", "40", "-n", "10", str(src)], capture_output=True, text=True,
+                       cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    used = frames[:10]
+    n = used.shape[1]
+    with smip.Stack(n, n, 20) as st:
+        st.push_frames(used)
+        ref_dat = tmp_path / "ref.dat"
+        st.save_bispectrum(str(ref_dat))
+        img, ph, fl, cons = st.finish(40.0)
+        sm, pw = st.sum(), st.power()
+    assert open(tmp_path / "bispectrum.dat", "rb").read() == open(ref_dat, "rb").read()
+    win = smip.hann(n, n, 80.0)
+
+    def gray(v):
+        return np.clip(v * 65535.0, 0, 65535).astype(np.uint16)
+
+    def shift(a):  # signed_symmetry: pixel (x, y) shows element (x - n/2, y - n/2)
+        return np.roll(a, (n // 2, n // 2), axis=(0, 1))
+
+    exp = {
+        "sum_image.png": gray(np.abs(sm / 255.0)),
+        "reco_image.png": gray(shift(np.abs(img))),
+        "phases.png": gray(shift((np.angle(ph * win) + np.pi) / (2 * np.pi))),
+        "powerspec.png": gray(shift(np.abs(pw / (np.abs(pw).max() / 1000.0)))),
+    }
+    for name, e in exp.items():
+        got = read_png16(tmp_path / name)
+        assert got.shape == e.shape
+        assert np.abs(got.astype(np.int64) - e.astype(np.int64)).max() <= 1, name
+    for name in ("sum_image_falsecolor.png", "phases_falsecolor.png", "phasecons.png", "powerspec_falsecolor.png",
+                 "reco_image_falsecolor.png"):
+        assert read_png16(tmp_path / name).shape == (n, n, 3)
+
+
+@pytest.mark.gpu
+def test_cpp_layer_matches_binding(smip, tmp_path):
+    """The C++ layer's Stack, Bispectrum, reconstruct_phases, CrossCorrelation,
+    Hann and NextRecoIndex against the binding on the same inputs."""
+    exe = _build_api_check(str(tmp_path))
+    r = subprocess.run([exe, str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0 and "ok" in r.stdout, (r.returncode, r.stdout, r.stderr)
+    # the same frames: std::mt19937(5) outputs % 4096, 6 frames of 64x64, row-major
+    # (numpy's legacy RandomState is the same MT19937 with the same integer seeding)
+    vals = np.random.RandomState(5).randint(0, 2 ** 32, size=6 * 64 * 64, dtype=np.uint32)
+    frames = (vals % 4096).astype(np.float64).reshape(6, 64, 64)
+    dx, dy = np.fromfile(tmp_path / "xc_shift.bin", np.int32)
+    assert (dx, dy) == smip.CrossCorrelation(frames[0])(frames[1])
+    with smip.Stack(64, 64, 20) as st:
+        st.push_frames(frames)
+        b = st.bispectrum()
+        ph, fl, _ = st.reconstruct_phases(24.0)
+    assert np.array_equal(np.fromfile(tmp_path / "stack_bispec.bin", np.complex64), b)
+    assert np.array_equal(np.fromfile(tmp_path / "stack_phases.bin", np.complex128), ph.ravel())
+    assert np.array_equal(np.fromfile(tmp_path / "stack_flags.bin", np.uint8), fl.ravel())
+    assert tuple(np.fromfile(tmp_path / "next_reco.bin", np.int32)) == smip.next_reco_index(0.0, 0.0, 0, 0)[2:]
+    assert np.array_equal(np.fromfile(tmp_path / "hann.bin", np.float64), smip.hann(64, 64, 48.0).ravel())

@@ -80,8 +80,21 @@ def test_extended256_sample(smip, oracle):
     check_against(out, exp, fp64_bispec=exp["bispec"])
 
 
+def test_default_depth_pipeline(smip, oracle):
+    """smip-cli's default depth -b 20 (not a multiple of 8) through the whole
+    pipeline, 128x128 u8 binary star, against the FP64 oracle."""
+    from smip_gb300 import synthetic as S
+
+    spec = S.config_spec("binary128", nframes=12)
+    frames = S.make_stack(spec)
+    exp = oracle.run_stack(frames, 20, 40.0, fp64=True, nthreads=16)
+    out = run_gpu(smip, frames, 20, 40.0, batch=8)
+    check_against(out, exp, fp64_bispec=exp["bispec"])
+
+
 @pytest.mark.parametrize("W,H,D", [(16, 16, 8), (32, 64, 16), (64, 32, 24), (64, 64, 32), (128, 64, 40),
-                                   (128, 128, 48), (128, 128, 56), (128, 128, 64), (64, 64, 9)])
+                                   (128, 128, 48), (128, 128, 56), (128, 128, 64), (64, 64, 9),
+                                   (16, 16, 2), (32, 32, 6), (64, 64, 20), (128, 64, 30), (64, 128, 46)])
 def test_accumulate_fft_shapes(smip, oracle, W, H, D):
     """Bispectrum::accumulate_from_fft for every supported depth, rectangular
     frames and an odd depth (behaves as depth-1), against FP64."""
@@ -249,6 +262,40 @@ def test_save_bispectrum_format(smip, tmp_path):
     hdr = np.frombuffer(raw[:40], np.uint64)
     assert list(hdr) == [B.size, 32, 32, 8, 8]
     assert np.array_equal(np.frombuffer(raw[40:], np.complex64), B)
+
+
+def test_load_bispectrum_resume(smip, tmp_path):
+    """bispectrum.dat written by one stack and read back into another: the
+    phase map is identical, and accumulation resumes where it stopped."""
+    rng = np.random.default_rng(7)
+    W = H = 64
+    D = 16
+    spec = np.fft.fft2(rng.integers(0, 4096, (6, H, W)).astype(float), axes=(1, 2))
+    fn = str(tmp_path / "bispectrum.dat")
+    with smip.Stack(W, H, D) as a:
+        a.accumulate_from_fft(spec[:4])
+        a.save_bispectrum(fn)
+        ph_a, fl_a, _ = a.reconstruct_phases(20)
+        b4 = a.bispectrum()
+        a.accumulate_from_fft(spec[4:])
+        b6 = a.bispectrum()
+    with smip.Stack(W, H, D) as b:
+        b.load_bispectrum(fn)
+        assert b.nframes == 1
+        assert np.array_equal(b.bispectrum(), b4)
+        ph_b, fl_b, _ = b.reconstruct_phases(20)
+        assert np.array_equal(fl_b, fl_a) and np.array_equal(ph_b, ph_a)
+    with smip.Stack(W, H, D) as c:
+        c.load_bispectrum(fn, nframes=4)
+        c.accumulate_from_fft(spec[4:])
+        assert c.nframes == 6
+        assert rel_l2(c.bispectrum(), b6) <= 1e-6
+        with pytest.raises(smip.InvalidArgument):
+            c.push_frames(np.zeros((1, H, W), np.uint16))
+    with smip.Stack(W, H, 24) as d, pytest.raises(smip.InvalidArgument):
+        d.load_bispectrum(fn)
+    with smip.Stack(W, H, D) as e, pytest.raises(smip.RuntimeFailure):
+        e.load_bispectrum(str(tmp_path / "missing.dat"))
 
 
 def test_full_size_properties(smip):
