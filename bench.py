@@ -208,6 +208,48 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+BATCHED_DESC = ("64 independent stacks queued at once: frame size from {64,128,256}, frames uniform in 50-1000, "
+                "binary u8 / extended u16 objects 50/50, depth 16/24/32 by size, reco radius 2 x depth")
+SERVED_DESC = ("Poisson arrivals at 20 jobs/s, 40 jobs, frame size from {64,128,256}, 100-2000 frames per job "
+               "delivered in 32-frame chunks, admission by bispectrum bytes under a 120 GB budget")
+
+
+def make_serving_jobs(procs):
+    """Jobs of the batched (64 stacks at once) and served (Poisson) workloads;
+    their frame banks are generated here, before any CUDA call."""
+    from smip_gb300 import serve
+
+    batched = serve.make_jobs(64, counts=(50, 1000), rate=None, seed=3000, bank_frames=256, procs=procs)
+    served = serve.make_jobs(40, counts=(100, 2000), rate=20.0, seed=4000, bank_frames=256, procs=procs)
+    return batched, served
+
+
+def serving_metrics(jobs):
+    """Batched and served execution against the plain single-job path on the
+    same jobs: frames/s, p50/p99 job latency, and whether every job's results
+    are identical in both."""
+    from smip_gb300 import serve
+
+    batched, served = jobs
+    keep = serve.pin_banks(batched + served)
+    shapes = {j.shape for j in batched + served}
+    out = {}
+    for key, jl, realtime, desc in (("batched", batched, False, BATCHED_DESC), ("served", served, True, SERVED_DESC)):
+        eng = serve.Engine(budget_bytes=120e9, max_active=32, workers=8)
+        eng.prewarm(shapes, count=12)
+        serve.run_plain(jl[:3], realtime=False)  # warm the code paths
+        res_s, span_s = eng.run(jl, realtime=realtime)
+        res_p, span_p = serve.run_plain(jl, realtime=realtime)
+        s, p = serve.summarize(res_s, span_s), serve.summarize(res_p, span_p)
+        out[key] = {"workload": desc, "served": s, "plain": p,
+                    "frames_per_s_ratio": s["frames_per_s"] / p["frames_per_s"],
+                    "results_identical": serve.compare_results(res_s, res_p),
+                    "peak_jobs_in_flight": eng.peak_active}
+        del eng
+    del keep
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -220,7 +262,11 @@ def run_ours(args):
     spec = S.config_spec(WORKLOAD, nframes=args.nframes, seed=replica_seed(2000, rank))
     # frames first (spawn pool before any CUDA call)
     t_gen = time.perf_counter()
-    frames = gen_frames(spec, args.nframes, min(16, os.cpu_count() or 1))
+    procs = min(16, os.cpu_count() or 1)
+    frames = gen_frames(spec, args.nframes, procs)
+    serve_jobs = None
+    if rank == 0 and world == 1 and not args.no_serve:
+        serve_jobs = make_serving_jobs(procs)
     t_gen = time.perf_counter() - t_gen
 
     torch.cuda.set_device(local)
@@ -329,6 +375,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(frames, D)
+    serving = serving_metrics(serve_jobs) if serve_jobs else None
     line = {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
@@ -342,6 +389,8 @@ def run_ours(args):
         "bispec_kernel_frames_per_s": (k2_frames / (k2_ms * 1e-3)) if k2_ms > 0 else None,
         "frame_generation_s": t_gen,
     }
+    if serving:
+        line.update(serving)
     st.close()
     if rank == 0:
         print(json.dumps(line))
@@ -357,6 +406,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nframes", type=int, default=2000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip the batched and served measurements")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -1,0 +1,326 @@
+"""Batched and served execution of many speckle-masking jobs on one GPU.
+
+The reference runs one job per ``smip-cli`` process (smip-cli/main.cpp:232-376);
+a job's accumulators are additive and independent of every other job's.  Here
+many jobs share one device:
+
+* every job owns a device-resident stack (packed bispectrum + compensation,
+  power spectrum, shift-and-add sum, reference frame) running on its own CUDA
+  stream, so the kernels of different jobs overlap on the GPU;
+* **continuous batching**: a request loop admits arriving jobs while slots and
+  bispectrum memory are free (admission is by bispectrum bytes under a budget),
+  streams every admitted job's frames in chunks, round robin, and hands a job
+  whose frames are all in to a worker thread for phase recovery and the final
+  image, while the loop keeps feeding the others;
+* stacks are pooled by shape and reset between jobs, so the loop allocates no
+  device memory after warm-up.
+
+``run_plain`` is the single-job path (one job at a time, in arrival order)
+that the served numbers are compared with.  A job's results do not depend on
+what else runs: each stack batches its own frames the same way alone and in a
+mix, so results are identical, which ``tests/test_serve.py`` checks.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import time
+from dataclasses import dataclass, field
+from typing import Callable, Dict, List, Optional, Tuple
+
+import numpy as np
+
+
+class FrameRing:
+    """``count`` frames read cyclically from a frame bank starting at
+    ``offset`` (no copy; the bank may be page-locked host memory)."""
+
+    def __init__(self, bank: np.ndarray, offset: int, count: int):
+        self.bank, self.offset, self.count = bank, int(offset), int(count)
+        self.shape = (self.count,) + bank.shape[1:]
+
+    def __len__(self):
+        return self.count
+
+    def parts(self, pos: int, k: int):
+        """Contiguous pieces holding frames [pos, pos + k)."""
+        out, n = [], len(self.bank)
+        while k > 0:
+            i = (self.offset + pos) % n
+            m = min(k, n - i)
+            out.append(self.bank[i:i + m])
+            pos, k = pos + m, k - m
+        return out
+
+    def materialize(self) -> np.ndarray:
+        return np.concatenate(self.parts(0, self.count))
+
+
+@dataclass
+class Job:
+    """One reconstruction request: frames plus smip-cli's -b and -p."""
+
+    id: int
+    frames: object              # [nframes][rows][cols] array (u8/u16/f32/f64) or a FrameRing
+    bdepth: int
+    reco_radius: float
+    arrival: float = 0.0        # seconds after the run starts
+    chunk: int = 32             # frames delivered per push
+
+    @property
+    def shape(self) -> Tuple[int, int, int]:
+        return (self.frames.shape[2], self.frames.shape[1], self.bdepth)
+
+    def parts(self, pos: int, k: int):
+        if isinstance(self.frames, FrameRing):
+            return self.frames.parts(pos, k)
+        return [self.frames[pos:pos + k]]
+
+
+@dataclass
+class JobResult:
+    id: int
+    nframes: int
+    arrival: float
+    admitted: float
+    done: float
+    image: np.ndarray = field(repr=False)
+    phases: np.ndarray = field(repr=False)
+    flags: np.ndarray = field(repr=False)
+    consistency: np.ndarray = field(repr=False)
+    shifts: np.ndarray = field(repr=False)
+
+    @property
+    def latency(self) -> float:
+        return self.done - self.arrival
+
+
+def bispectrum_bytes(ncols: int, nrows: int, bdepth: int) -> int:
+    """Device bytes of one job's bispectrum: the packed accumulator, its Kahan
+    compensation and the normalised copy (complex<float> each)."""
+    d = (bdepth // 2) * 2
+    base = (ncols // 2 + 1) * (nrows + 1) * (d // 2 + 1) * (d + 1)
+    return 3 * 8 * base
+
+
+def summarize(results: List[JobResult], makespan: float) -> dict:
+    lat = np.array([r.latency for r in results]) * 1e3
+    frames = sum(r.nframes for r in results)
+    return {"jobs": len(results), "frames": frames, "seconds": makespan, "frames_per_s": frames / makespan,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
+
+
+class Engine:
+    """Continuous-batching request loop over a pool of device-resident stacks.
+
+    budget_bytes: admission budget in bispectrum bytes (``bispectrum_bytes``).
+    max_active: jobs in flight at once (streaming or reconstructing).
+    workers: threads that run phase recovery + the final image.
+    stack_factory: (ncols, nrows, bdepth) -> stack; defaults to smip_gb300.Stack.
+    """
+
+    def __init__(self, device: int = 0, budget_bytes: float = 120e9, max_active: int = 24, workers: int = 4,
+                 stack_factory: Optional[Callable] = None):
+        if stack_factory is None:
+            from smip_gb300 import Stack
+
+            def stack_factory(nc, nr, d):
+                return Stack(nc, nr, d, device=device)
+        self.factory = stack_factory
+        self.budget = float(budget_bytes)
+        self.max_active = int(max_active)
+        self.workers = int(workers)
+        self.pool: Dict[Tuple[int, int, int], list] = {}
+        self.peak_bytes = 0.0
+        self.peak_active = 0
+
+    def prewarm(self, shapes, count: int = 1):
+        """Creates ``count`` pooled stacks per (ncols, nrows, bdepth) shape, so
+        that no device allocation happens while jobs are served."""
+        for s in shapes:
+            lst = self.pool.setdefault(tuple(s), [])
+            while len(lst) < count:
+                lst.append(self.factory(*s))
+
+    def _acquire(self, shape):
+        lst = self.pool.setdefault(shape, [])
+        return lst.pop() if lst else self.factory(*shape)
+
+    def _release(self, shape, st):
+        st.reset()
+        self.pool[shape].append(st)
+
+    @staticmethod
+    def _finish(job: Job, st, t0: float, admitted: float) -> JobResult:
+        img, ph, fl, cs = st.finish(job.reco_radius)
+        sh = st.shifts()
+        return JobResult(job.id, len(job.frames), job.arrival, admitted, time.perf_counter() - t0, img, ph, fl, cs, sh)
+
+    def run(self, jobs: List[Job], realtime: bool = True) -> Tuple[List[JobResult], float]:
+        """Serves ``jobs``; with ``realtime`` a job is only visible from its
+        arrival time on, otherwise all are queued at once (batched mode).
+        Returns (results in completion order, makespan in seconds)."""
+        waiting = sorted(jobs, key=lambda j: (j.arrival, j.id))
+        active: list = []          # [job, stack, frames pushed, admitted time, bytes]
+        running: dict = {}         # future -> (job, stack, bytes)
+        results: List[JobResult] = []
+        used = 0.0
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=self.workers) as ex:
+            while waiting or active or running:
+                now = time.perf_counter() - t0
+                # admission: FIFO, by slots and bispectrum bytes
+                while waiting and (not realtime or waiting[0].arrival <= now) \
+                        and len(active) + len(running) < self.max_active:
+                    job = waiting[0]
+                    need = bispectrum_bytes(*job.shape)
+                    if used + need > self.budget and (active or running):
+                        break
+                    waiting.pop(0)
+                    used += need
+                    active.append([job, self._acquire(job.shape), 0, now, need])
+                self.peak_bytes = max(self.peak_bytes, used)
+                self.peak_active = max(self.peak_active, len(active) + len(running))
+                # one chunk per streaming job, round robin
+                pushed = False
+                for entry in list(active):
+                    job, st, pos = entry[0], entry[1], entry[2]
+                    k = min(job.chunk, len(job.frames) - pos)
+                    for part in job.parts(pos, k):
+                        st.push_frames(part)
+                    entry[2] = pos + k
+                    pushed = True
+                    if entry[2] == len(job.frames):
+                        active.remove(entry)
+                        fut = ex.submit(self._finish, job, st, t0, entry[3])
+                        running[fut] = (job, st, entry[4])
+                # completions
+                done = [f for f in running if f.done()]
+                for f in done:
+                    job, st, need = running.pop(f)
+                    results.append(f.result())
+                    self._release(job.shape, st)
+                    used -= need
+                if not pushed and not done:
+                    if running:
+                        cf.wait(list(running), timeout=0.002, return_when=cf.FIRST_COMPLETED)
+                    elif waiting:
+                        time.sleep(max(0.0, min(0.002, waiting[0].arrival - (time.perf_counter() - t0))))
+        return results, time.perf_counter() - t0
+
+
+def run_plain(jobs: List[Job], device: int = 0, realtime: bool = True,
+              stack_factory: Optional[Callable] = None) -> Tuple[List[JobResult], float]:
+    """The single-job path: one job at a time in arrival order, each pushed
+    completely and reconstructed before the next starts (one pooled stack per
+    shape)."""
+    if stack_factory is None:
+        from smip_gb300 import Stack
+
+        def stack_factory(nc, nr, d):
+            return Stack(nc, nr, d, device=device)
+    pool: dict = {}
+    results = []
+    t0 = time.perf_counter()
+    for job in sorted(jobs, key=lambda j: (j.arrival, j.id)):
+        if realtime:
+            wait = job.arrival - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+        st = pool.get(job.shape)
+        if st is None:
+            st = pool[job.shape] = stack_factory(*job.shape)
+        admitted = time.perf_counter() - t0
+        for pos in range(0, len(job.frames), job.chunk):
+            for part in job.parts(pos, min(job.chunk, len(job.frames) - pos)):
+                st.push_frames(part)
+        results.append(Engine._finish(job, st, t0, admitted))
+        st.reset()
+    return results, time.perf_counter() - t0
+
+
+# ------------------------------------------------------------- workloads
+def _bank(n: int, kind: str, count: int, seed: int, procs: int = 1):
+    from smip_gb300 import synthetic as S
+
+    spec = S.StackSpec(n=n, nframes=count, kind=kind, dtype="uint8" if kind == "binary" else "uint16",
+                       d_over_r0=10.0 if kind == "binary" else 15.0, seed=seed)
+    if procs <= 1:
+        return S.make_stack(spec, 0, count)
+    import multiprocessing as mp
+
+    step = (count + procs - 1) // procs
+    parts = [(spec, s, min(step, count - s)) for s in range(0, count, step)]
+    with mp.get_context("spawn").Pool(procs) as pool:
+        return np.concatenate(pool.starmap(S.make_stack, parts))
+
+
+def depth_for(n: int) -> int:
+    """Bispectrum depth scaled per stack size: 16 at 64^2, 24 at 128^2, 32 at 256^2."""
+    return {64: 16, 128: 24, 256: 32}[n]
+
+
+def make_jobs(njobs: int, sizes=(64, 128, 256), counts=(50, 1000), rate: Optional[float] = None,
+              seed: int = 3000, bank_frames: int = 256, procs: int = 1, chunk: int = 32,
+              pin: bool = False) -> List[Job]:
+    """Uneven jobs: frame size drawn from ``sizes``, frame count uniform in
+    ``counts``, binary or extended objects 50/50, depth scaled per size and
+    reco radius 2 x depth (smip-cli's default ratio).  A job's frames are a
+    cyclic run through a seeded per-(size, kind) frame bank.  ``rate``:
+    Poisson arrivals (jobs/s), else all arrive at t = 0.  ``pin``: banks in
+    page-locked host memory (torch), so pushes are asynchronous."""
+    rng = np.random.default_rng(seed)
+    plan = []
+    t = 0.0
+    for i in range(njobs):
+        n = int(rng.choice(sizes))
+        kind = "binary" if rng.uniform() < 0.5 else "extended"
+        cnt = int(rng.integers(counts[0], counts[1] + 1))
+        off = int(rng.integers(0, bank_frames))
+        if rate:
+            t += float(rng.exponential(1.0 / rate))
+        plan.append((i, n, kind, cnt, off, t if rate else 0.0))
+    banks = {}
+    for key in sorted({(n, kind) for _, n, kind, _, _, _ in plan}):
+        n, kind = key
+        b = _bank(n, kind, bank_frames, seed + 7 * n + (kind == "extended"), procs)
+        if pin:
+            import torch
+
+            tt = torch.from_numpy(np.ascontiguousarray(b)).pin_memory()
+            banks[key] = (tt.numpy(), tt)  # the tensor keeps the page-locked memory alive
+        else:
+            banks[key] = (b, None)
+    jobs = []
+    for i, n, kind, cnt, off, arr in plan:
+        d = depth_for(n)
+        job = Job(i, FrameRing(banks[(n, kind)][0], off, cnt), d, 2.0 * d, arrival=arr, chunk=chunk)
+        job.bank_owner = banks[(n, kind)][1]
+        jobs.append(job)
+    return jobs
+
+
+def pin_banks(jobs: List[Job]):
+    """Moves the jobs' frame banks into page-locked host memory (torch), so
+    pushes from them are asynchronous; returns the owners to keep alive."""
+    import torch
+
+    pinned, owners = {}, []
+    for job in jobs:
+        fr = job.frames
+        if not isinstance(fr, FrameRing):
+            continue
+        key = id(fr.bank)
+        if key not in pinned:
+            tt = torch.from_numpy(np.ascontiguousarray(fr.bank)).pin_memory()
+            pinned[key] = tt.numpy()
+            owners.append(tt)
+        fr.bank = pinned[key]
+    return owners
+
+
+def compare_results(a: List[JobResult], b: List[JobResult]) -> bool:
+    """True when every job has bit-identical shifts, flags, phases and image."""
+    bb = {r.id: r for r in b}
+    return all(np.array_equal(r.shifts, bb[r.id].shifts) and np.array_equal(r.flags, bb[r.id].flags)
+               and np.array_equal(r.phases, bb[r.id].phases) and np.array_equal(r.image, bb[r.id].image)
+               for r in a)

@@ -1,0 +1,104 @@
+"""Batched/served execution (smip_gb300/serve.py): admission by bispectrum
+bytes, continuous batching, and -- on the GPU -- that every job's results are
+the same alone and in a mix."""
+import numpy as np
+import pytest
+
+from smip_gb300 import serve
+
+
+class FakeStack:
+    """Host stand-in for smip_gb300.Stack: records pushes, returns a result
+    that depends only on the job's own frames."""
+
+    live = 0
+
+    def __init__(self, nc, nr, d):
+        self.shape = (nc, nr, d)
+        self.frames = []
+        FakeStack.live += 1
+
+    def push_frames(self, f):
+        self.frames.append(np.array(f))
+
+    def finish(self, R):
+        a = np.concatenate(self.frames).astype(np.float64)
+        s = a.sum(axis=0) + R
+        return s.astype(np.complex128), s.astype(np.complex128), (s > 0).astype(np.uint8), s
+
+    def shifts(self):
+        return np.zeros((sum(len(f) for f in self.frames), 2), np.int32)
+
+    def reset(self):
+        self.frames = []
+
+
+def _jobs(n, rate=None, seed=1):
+    rng = np.random.default_rng(seed)
+    out, t = [], 0.0
+    for i in range(n):
+        sz = int(rng.choice([16, 32]))
+        fr = rng.integers(0, 255, (int(rng.integers(3, 70)), sz, sz)).astype(np.uint8)
+        if rate:
+            t += float(rng.exponential(1.0 / rate))
+        out.append(serve.Job(i, fr, 8, 6.0, arrival=t if rate else 0.0, chunk=16))
+    return out
+
+
+def test_bispectrum_bytes_matches_layout():
+    from oracle import bispec_desc
+
+    for n, d in ((64, 16), (128, 24), (256, 32), (64, 9)):
+        assert serve.bispectrum_bytes(n, n, d) == 3 * 8 * bispec_desc(n, n, d)["base_size"]
+
+
+def test_engine_admission_and_results():
+    jobs = _jobs(20)
+    budget = 3 * serve.bispectrum_bytes(32, 32, 8)  # at most three jobs' bispectra
+    eng = serve.Engine(budget_bytes=budget, max_active=8, workers=2, stack_factory=FakeStack)
+    res, span = eng.run(jobs, realtime=False)
+    assert sorted(r.id for r in res) == list(range(20))
+    assert eng.peak_bytes <= budget and eng.peak_active <= 8
+    plain, _ = serve.run_plain(jobs, realtime=False, stack_factory=FakeStack)
+    by_id = {r.id: r for r in plain}
+    for r in res:
+        assert np.array_equal(r.image, by_id[r.id].image) and r.nframes == len(jobs[r.id].frames)
+    s = serve.summarize(res, span)
+    assert s["jobs"] == 20 and s["frames"] == sum(len(j.frames) for j in jobs)
+
+
+def test_engine_realtime_respects_arrivals():
+    jobs = _jobs(8, rate=200.0)
+    eng = serve.Engine(max_active=4, workers=2, stack_factory=FakeStack)
+    res, _ = eng.run(jobs, realtime=True)
+    for r in res:
+        assert r.admitted >= r.arrival - 1e-9 and r.done >= r.admitted
+
+
+def test_engine_pool_reuses_stacks():
+    FakeStack.live = 0
+    jobs = _jobs(12)
+    eng = serve.Engine(max_active=2, workers=1, stack_factory=FakeStack)
+    eng.prewarm({j.shape for j in jobs}, count=2)
+    made = FakeStack.live
+    eng.run(jobs, realtime=False)
+    assert FakeStack.live == made  # no stack created while serving
+
+
+@pytest.mark.gpu
+def test_results_same_alone_and_in_mix(smip):
+    """Jobs of mixed sizes (64^2 binary u8, 128^2 extended u16, uneven counts)
+    served concurrently give exactly the results each gives alone."""
+    jobs = serve.make_jobs(6, sizes=(64, 128), counts=(30, 300), bank_frames=64, seed=11)
+    eng = serve.Engine(max_active=6, workers=3)
+    eng.prewarm({j.shape for j in jobs}, count=3)
+    mixed, _ = eng.run(jobs, realtime=False)
+    alone, _ = serve.run_plain(jobs, realtime=False)
+    by_id = {r.id: r for r in alone}
+    assert eng.peak_active >= 2
+    for r in mixed:
+        a = by_id[r.id]
+        assert np.array_equal(r.shifts, a.shifts)
+        assert np.array_equal(r.flags, a.flags)
+        assert np.array_equal(r.phases, a.phases)
+        assert np.array_equal(r.image, a.image)
