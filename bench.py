@@ -235,8 +235,8 @@ def serving_metrics(jobs):
     shapes = {j.shape for j in batched + served}
     out = {}
     for key, jl, realtime, desc in (("batched", batched, False, BATCHED_DESC), ("served", served, True, SERVED_DESC)):
-        eng = serve.Engine(budget_bytes=120e9, max_active=32, workers=8)
-        eng.prewarm(shapes, count=12)
+        eng = serve.Engine(budget_bytes=120e9, max_active=64, workers=32)
+        eng.prewarm(shapes, count=24)
         serve.run_plain(jl[:3], realtime=False)  # warm the code paths
         res_s, span_s = eng.run(jl, realtime=realtime)
         res_p, span_p = serve.run_plain(jl, realtime=realtime)

@@ -118,7 +118,7 @@ class Engine:
     stack_factory: (ncols, nrows, bdepth) -> stack; defaults to smip_gb300.Stack.
     """
 
-    def __init__(self, device: int = 0, budget_bytes: float = 120e9, max_active: int = 24, workers: int = 4,
+    def __init__(self, device: int = 0, budget_bytes: float = 120e9, max_active: int = 64, workers: int = 32,
                  stack_factory: Optional[Callable] = None):
         if stack_factory is None:
             from smip_gb300 import Stack
