@@ -90,6 +90,13 @@ struct BispecArgs {
     int njt;      // j tiles: ceil(H / JT)
     int nmain;    // main tiles
     int ntiles;   // main + row-0 tiles
+    // Work split (stream-K style): every CTA runs R whole tiles b + k*G; the
+    // last ntiles - R*G tiles are split by frames into P parts each, one part
+    // per CTA b < nsplit.  Parts write partial sums to scratch; the CTA that
+    // completes a tile's last part adds the parts, in part order, into (B, C).
+    int G, R, P, nsplit;
+    float2* scratch;   // [nsplit][NSLOT][THREADS] partial sums
+    int* tile_cnt;     // [ntiles - R*G] parts finished (zero between launches)
 };
 
 // Tile geometry shared by the TMA issue path and the consumers.
@@ -131,7 +138,9 @@ __device__ __forceinline__ void cmac(float2& acc, float2 a, float2 v, float2 w)
     acc.y = fmaf(ti, w.x, fmaf(-tr, w.y, acc.y));
 }
 
-template <int DE>
+// EXACT: the stack's depth is DE itself (compile-time layout); otherwise the
+// depth comes from the arguments (BispecArgs::D < DE).
+template <int DE, bool EXACT>
 __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
     bispec_accum_kernel(const __grid_constant__ CUtensorMap tmW, const __grid_constant__ CUtensorMap tmV,
                         const __grid_constant__ CUtensorMap tmA, const BispecArgs p)
@@ -151,17 +160,32 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
     }
     __syncthreads();
     const int half_h = p.H / 2;
-    const int my_tiles = p.ntiles > (int)blockIdx.x ? (p.ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-    const uint32_t total = (uint32_t)my_tiles * (uint32_t)p.nframes;
+    const int nf = p.nframes;
+    // this CTA's units: R whole tiles b + k*G, then (if b < nsplit) part
+    // b % P of split tile R*G + b / P, frames [part*nf/P, (part+1)*nf/P)
+    auto split_tile = [&]() { return p.R * p.G + (int)blockIdx.x / p.P; };
+    auto split_f0 = [&]() { return (int)((long long)((int)blockIdx.x % p.P) * nf / p.P); };
+    auto split_f1 = [&]() { return (int)((long long)((int)blockIdx.x % p.P + 1) * nf / p.P); };
+    const bool has_split = (int)blockIdx.x < p.nsplit;
+    const int my_units = p.R + (has_split ? 1 : 0);
+    const uint32_t total = (uint32_t)p.R * (uint32_t)nf + (has_split ? (uint32_t)(split_f1() - split_f0()) : 0u);
     const int cv = (half_h - DE / 2) & ~1;
     const int offv = (half_h - DE / 2) - cv;
 
     // issue the loads of iteration r (tile r / nframes, frame r % nframes) into stage r % NS;
     // box x coordinates are in 8-byte elements and even (16-byte aligned)
     auto issue = [&](uint32_t r) {
-        const uint32_t k = r / p.nframes;
-        const int f = (int)(r - k * p.nframes);
-        const TileInfo ti = decode_tile<DE>((int)blockIdx.x + (int)k * (int)gridDim.x, p);
+        int f, t;
+        const uint32_t full_iters = (uint32_t)p.R * (uint32_t)nf;
+        if (r < full_iters) {
+            const uint32_t k = r / nf;
+            f = (int)(r - k * nf);
+            t = (int)blockIdx.x + (int)k * p.G;
+        } else {
+            f = split_f0() + (int)(r - full_iters);
+            t = split_tile();
+        }
+        const TileInfo ti = decode_tile<DE>(t, p);
         const int cw = (ti.j0 + half_h - DE / 2) & ~1;
         const int s = r % Cf::NS;
         unsigned char* st = smem + s * Cf::STAGE;
@@ -198,8 +222,11 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
     const bool edge = lb == Cf::NLB - 1;
     uint32_t r = 0;
     bool ok = true;
-    for (int k = 0; k < my_tiles && ok; ++k) {
-        const TileInfo ti = decode_tile<DE>((int)blockIdx.x + k * (int)gridDim.x, p);
+    __shared__ int s_last; // this CTA completes its split tile
+    for (int k = 0; k < my_units && ok; ++k) {
+        const bool split_unit = k == p.R;       // the part of a split tile
+        const int nfu = split_unit ? split_f1() - split_f0() : nf; // frames of this unit
+        const TileInfo ti = decode_tile<DE>(split_unit ? split_tile() : (int)blockIdx.x + k * p.G, p);
         const int a0 = ti.row0 ? ti.a0 + wr : ti.a0;
         const int a2 = ti.row0 ? 0 : 1 + ti.c * Cf::RPC + wr;
         const int vrow = ti.row0 ? 0 : wr;
@@ -219,7 +246,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
                 acc[a][b] = make_float2(0.f, 0.f);
         float2 acce = make_float2(0.f, 0.f);
 
-        for (int f = 0; f < p.nframes; ++f, ++r) {
+        for (int f = 0; f < nfu; ++f, ++r) {
             const int s = r % Cf::NS;
             // every lane waits; the warp leaves together if any lane timed out
             const bool got = mbar_wait_bounded(&full[s], (r / Cf::NS) & 1, kWaitNs);
@@ -282,18 +309,63 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
         }
         if (!ok)
             break;
-        const int hd = p.D / 2; // a depth below DE computes the template's extra rows and columns, stores none
-        if (a0 < p.hw && jw < half_h && a2 <= hd) {
+        if (split_unit && p.P > 1) {
+            // write this part's sums; the CTA that finishes the tile's last part merges
+            constexpr int NSLOT = 8 * Cf::TLW + 1;
+            const int b = (int)blockIdx.x, s_part = b % p.P, s_tile = split_tile();
+            float2* sc = p.scratch + (long long)b * NSLOT * Cf::THREADS + threadIdx.x;
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+#pragma unroll
+                for (int q = 0; q < Cf::TLW; ++q)
+                    sc[(a * Cf::TLW + q) * Cf::THREADS] = acc[a][q];
+            sc[(NSLOT - 1) * Cf::THREADS] = acce;
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0)
+                s_last = atomicAdd(&p.tile_cnt[s_tile - p.R * p.G], 1) == p.P - 1;
+            __syncthreads();
+            if (!s_last)
+                continue;
+            __threadfence();
+            // parts in order 0..P-1: a fixed summation order whichever CTA merges
+            const float2* sb = p.scratch + (long long)(b - s_part) * NSLOT * Cf::THREADS + threadIdx.x;
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+#pragma unroll
+                for (int q = 0; q < Cf::TLW; ++q)
+                    acc[a][q] = make_float2(0.f, 0.f);
+            acce = make_float2(0.f, 0.f);
+            for (int pp = 0; pp < p.P; ++pp) {
+                const float2* sp = sb + (long long)pp * NSLOT * Cf::THREADS;
+#pragma unroll
+                for (int a = 0; a < 8; ++a)
+#pragma unroll
+                    for (int q = 0; q < Cf::TLW; ++q) {
+                        const float2 v = __ldcg(sp + (a * Cf::TLW + q) * Cf::THREADS);
+                        acc[a][q].x += v.x;
+                        acc[a][q].y += v.y;
+                    }
+                const float2 v = __ldcg(sp + (NSLOT - 1) * Cf::THREADS);
+                acce.x += v.x;
+                acce.y += v.y;
+            }
+            if (threadIdx.x == 0)
+                p.tile_cnt[s_tile - p.R * p.G] = 0; // ready for the next launch
+        }
+        const int D = EXACT ? DE : p.D;
+        const int hd = D / 2; // a depth below DE computes the template's extra rows and columns, stores none
+        if (a0 < p.hw && jw < half_h && (EXACT || a2 <= hd)) {
             // Kahan-compensated add of the batch partial into (B, C); within a
             // j step every load is issued before the first store (B and C never
             // alias).
             const int H = p.H;
-            const int rowE = (hd + 1) * (p.D + 1);
-            float2* __restrict__ Bt = p.B + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (p.D + 1);
-            float2* __restrict__ Ct = p.C + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (p.D + 1);
+            const int rowE = (hd + 1) * (D + 1);
+            float2* __restrict__ Bt = p.B + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (D + 1);
+            float2* __restrict__ Ct = p.C + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (D + 1);
             auto off = [&](int j, int l) {
                 const int a1 = j >= 0 ? j : j + H + 1;
-                const int a3 = l >= 0 ? l : l + p.D + 1;
+                const int a3 = l >= 0 ? l : l + D + 1;
                 return a1 * rowE + a3;
             };
             auto kahan = [](float2& b, float2& c, float2 v) {
@@ -304,7 +376,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
                 b = make_float2(tx, ty);
             };
             // a tile may reach past j = H/2 - 1 when H < JT: those sums are zero and not stored
-            const bool has_e = edge && jw + lane < half_h && DE == p.D;
+            const bool has_e = edge && jw + lane < half_h && DE == D;
             const int oe = off(jw + lane, DE / 2);
             float2 be = make_float2(0.f, 0.f), ce = be;
             if (has_e) {
@@ -321,7 +393,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
 #pragma unroll
                     for (int b = 0; b < Cf::TLW; ++b) {
                         const int l = -DE / 2 + 8 * Cf::TLW * lb + lg + 8 * b;
-                        st[b] = b < nb && l >= -hd && l <= hd;
+                        st[b] = b < nb && (EXACT || (l >= -hd && l <= hd));
                         if (st[b]) {
                             o[b] = off(j, l);
                             bv[b] = Bt[o[b]];
@@ -391,7 +463,7 @@ static bool make_map(CUtensorMap* m, const float2* S, int nframes, const Geometr
         == CUDA_SUCCESS;
 }
 
-template <int DE>
+template <int DE, bool EXACT>
 static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStream_t st)
 {
     using Cf = BCfg<DE>;
@@ -399,7 +471,7 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
     if (!make_map(&mW, L.S, L.nframes, g, Cf::BW, Cf::RPC) || !make_map(&mV, L.S, L.nframes, g, Cf::BV, Cf::RPC)
         || !make_map(&mA, L.S, L.nframes, g, Cf::JT, 1))
         return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(bispec_accum_kernel<DE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(bispec_accum_kernel<DE, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          Cf::SMEM);
     if (e != cudaSuccess)
         return e;
@@ -415,12 +487,30 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
     a.njt = (g.H + Cf::JT - 1) / Cf::JT;
     a.nmain = g.hw * a.njt * a.nchm;
     a.ntiles = a.nmain + (g.hw + Cf::RPC - 1) / Cf::RPC * a.njt;
-    const int grid = a.ntiles < L.num_sms ? a.ntiles : L.num_sms;
-    bispec_accum_kernel<DE><<<grid, Cf::THREADS, Cf::SMEM, st>>>(mW, mV, mA, a); note_launches(1);
+    // Whole rounds of G tiles, then the remainder split by frames so that every
+    // CTA gets the same work (parts of at least 8 frames).
+    a.G = L.num_sms;
+    a.R = a.ntiles / a.G;
+    const int rem = a.ntiles - a.R * a.G;
+    int P = rem > 0 ? a.G / rem : 1;
+    P = P < 1 ? 1 : P;
+    const int pmax = L.nframes / 8 > 1 ? L.nframes / 8 : 1;
+    P = P > pmax ? pmax : P;
+    if (!L.scratch || !L.tile_cnt)
+        P = 1;
+    a.P = P;
+    a.nsplit = rem * P;
+    a.scratch = L.scratch;
+    a.tile_cnt = L.tile_cnt;
+    const int grid = a.R > 0 ? a.G : a.nsplit;
+    bispec_accum_kernel<DE, EXACT><<<grid, Cf::THREADS, Cf::SMEM, st>>>(mW, mV, mA, a); note_launches(1);
     return cudaGetLastError();
 }
 
 bool bispec_depth_supported(int De) { return De >= 2 && De <= 64 && De % 2 == 0; }
+
+// partial sums of one split-tile part: (8 j x 4 l + 1 edge) float2 per thread, 512 threads
+size_t bispec_scratch_bytes(int num_sms) { return (size_t)num_sms * 33 * 512 * sizeof(float2); }
 
 // The kernel is instantiated for depths that are multiples of 8; another even
 // depth runs the next one up and stores only its own elements.
@@ -428,15 +518,16 @@ cudaError_t launch_bispec_accumulate(const BispecLaunch& L, const Geometry& g, c
 {
     if (L.nframes <= 0)
         return cudaSuccess;
+    const bool exact = g.De % 8 == 0;
     switch ((g.De + 7) / 8 * 8) {
-    case 8: return launch_de<8>(L, g, st);
-    case 16: return launch_de<16>(L, g, st);
-    case 24: return launch_de<24>(L, g, st);
-    case 32: return launch_de<32>(L, g, st);
-    case 40: return launch_de<40>(L, g, st);
-    case 48: return launch_de<48>(L, g, st);
-    case 56: return launch_de<56>(L, g, st);
-    case 64: return launch_de<64>(L, g, st);
+    case 8: return exact ? launch_de<8, true>(L, g, st) : launch_de<8, false>(L, g, st);
+    case 16: return exact ? launch_de<16, true>(L, g, st) : launch_de<16, false>(L, g, st);
+    case 24: return exact ? launch_de<24, true>(L, g, st) : launch_de<24, false>(L, g, st);
+    case 32: return exact ? launch_de<32, true>(L, g, st) : launch_de<32, false>(L, g, st);
+    case 40: return exact ? launch_de<40, true>(L, g, st) : launch_de<40, false>(L, g, st);
+    case 48: return exact ? launch_de<48, true>(L, g, st) : launch_de<48, false>(L, g, st);
+    case 56: return exact ? launch_de<56, true>(L, g, st) : launch_de<56, false>(L, g, st);
+    case 64: return exact ? launch_de<64, true>(L, g, st) : launch_de<64, false>(L, g, st);
     default: return cudaErrorInvalidValue;
     }
 }

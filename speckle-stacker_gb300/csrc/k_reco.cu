@@ -7,7 +7,7 @@
 // u and v flagged, |B| > DBL_EPSILON, v inside the bispectrum's v range.
 // Each point may use phases set earlier in the same ring, so the walk is a
 // strict serial chain; the parallelism is inside a point: the (d+1)^2
-// candidate pairs are spread over the 1024 threads of the block.
+// candidate pairs are spread over the 512 threads of the block.
 //
 // Latency structure of one point: the bispectrum gathers depend only on w, not
 // on the chain, so the gathers of the NEXT point are issued before the
@@ -27,6 +27,7 @@ namespace smip_gpu {
 
 constexpr int kRecoThreads = 512;
 constexpr int kVisitChunk = 2048;
+constexpr int kSlots = (65 * 65 + kRecoThreads - 1) / kRecoThreads; // pair slots per thread (d <= 64)
 
 __device__ __forceinline__ int wrap_idx(int x, int y, int W, int H)
 {
@@ -170,14 +171,29 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_chain_kernel(const Reco
     const int umn0 = -(szW / 2), umx0 = szW - szW / 2 - 1, umn1 = -(szH / 2), umx1 = szH - szH / 2 - 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
-    // own slots t = threadIdx.x + k * blockDim.x; each thread reads only what it copied
+    // This thread's pair slots t = threadIdx.x + k * kRecoThreads and their v
+    // (and v's map index), computed once for the whole walk.
+    int svx[kSlots], svy[kSlots], spv[kSlots];
+#pragma unroll
+    for (int k = 0; k < kSlots; ++k) {
+        const int t = threadIdx.x + k * kRecoThreads;
+        svx[k] = -De / 2 + t % nside;
+        svy[k] = -De / 2 + t / nside;
+        spv[k] = t < nv ? wrap_idx(svx[k], svy[k], W, H) : 0;
+    }
+
+    // each thread copies its own slots and later reads only what it copied
     auto prefetch = [&](int q, int2 w, int buf) {
         const float2* row = J.plan + (long long)q * nv;
-        for (int t = threadIdx.x; t < nv; t += blockDim.x) {
-            cp_async8(&rowbuf[buf * nv + t], &row[t]);
-            const int ux = w.x - (-De / 2 + t % nside), uy = w.y - (-De / 2 + t / nside);
-            if (!(ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1))
-                cp_async8(&phubuf[buf * nv + t], &J.phf[wrap_idx(ux, uy, W, H)]);
+#pragma unroll
+        for (int k = 0; k < kSlots; ++k) {
+            const int t = threadIdx.x + k * kRecoThreads;
+            if (t < nv) {
+                cp_async8(&rowbuf[buf * nv + t], &row[t]);
+                const int ux = w.x - svx[k], uy = w.y - svy[k];
+                if (!(ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1))
+                    cp_async8(&phubuf[buf * nv + t], &J.phf[wrap_idx(ux, uy, W, H)]);
+            }
         }
         cp_async_commit();
     };
@@ -213,12 +229,15 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_chain_kernel(const Reco
                 const float2 lph = last_ph;
                 float sr = 0.f, si = 0.f;
                 int cnt = 0;
-                for (int t = threadIdx.x; t < nv; t += blockDim.x) {
+#pragma unroll
+                for (int k = 0; k < kSlots; ++k) {
+                    const int t = threadIdx.x + k * kRecoThreads;
+                    if (t >= nv)
+                        continue;
                     const float2 bh = rowbuf[buf * nv + t];
                     if (bh.x == 0.f && bh.y == 0.f)
                         continue;
-                    const int vx = -De / 2 + t % nside, vy = -De / 2 + t / nside;
-                    const int pu = wrap_idx(w.x - vx, w.y - vy, W, H), pv = wrap_idx(vx, vy, W, H);
+                    const int pu = wrap_idx(w.x - svx[k], w.y - svy[k], W, H), pv = spv[k];
                     if (!(flagbits[pu >> 5] & (1u << (pu & 31))) || !(flagbits[pv >> 5] & (1u << (pv & 31))))
                         continue;
                     if (isnan(bh.x)) {
@@ -246,12 +265,12 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_chain_kernel(const Reco
                 __syncthreads();
                 if (warp == 0) {
                     // float-float across warps: the mean phasor can be a large cancellation
-                    const int nw = blockDim.x >> 5;
+                    constexpr int nw = kRecoThreads / 32;
                     float rh = lane < nw ? red[0][lane] : 0.f, rl = 0.f;
                     float ih = lane < nw ? red[1][lane] : 0.f, il = 0.f;
                     cnt = lane < nw ? red_n[lane] : 0;
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) {
+                    for (int o = nw / 2; o > 0; o >>= 1) {
                         const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
                         const float c = __shfl_xor_sync(0xffffffffu, ih, o), e = __shfl_xor_sync(0xffffffffu, il, o);
                         ff_add(rh, rl, a, b);

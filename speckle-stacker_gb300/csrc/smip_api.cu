@@ -324,6 +324,8 @@ struct smip_stack {
     dfc* Gt = nullptr;            // row-FFT output, float-float
     float2 *T = nullptr, *S = nullptr, *R = nullptr;
     float* corr = nullptr;
+    float2* kscratch = nullptr;   // bispectrum kernel: partial sums of split tiles
+    int* ktile_cnt = nullptr;     // bispectrum kernel: parts finished per split tile
     int* shifts = nullptr;        // all frames, int2
     long shifts_cap = 0;
     int* err = nullptr;
@@ -343,6 +345,7 @@ struct smip_stack {
         dfree(spec_staging);
         if (ref) cudaFree(ref);
         dfree(ref_sq); dfree(Gt); dfree(T); dfree(S); dfree(R); dfree(corr); dfree(shifts); dfree(err);
+        dfree(kscratch); dfree(ktile_cnt);
         dfree(Z); dfree(pfull); dfree(maxbuf);
         for (auto& e : ev_pool) {
             cudaEventDestroy(e.first);
@@ -425,6 +428,11 @@ struct smip_stack {
             CUDA_TRY(launch_saa_add(dtype, sum, staging, (long long)fe, n, first ? 1 : 0, shifts + 2 * first_index, g, st));
             has_ref = true;
         }
+        if (!kscratch) {
+            CUDA_TRY(cudaMalloc(&kscratch, bispec_scratch_bytes(ctx->num_sms)));
+            CUDA_TRY(cudaMalloc(&ktile_cnt, sizeof(int) * ctx->num_sms));
+            CUDA_TRY(cudaMemsetAsync(ktile_cnt, 0, sizeof(int) * ctx->num_sms, st));
+        }
         BispecLaunch L;
         L.S = S;
         L.nframes = n;
@@ -432,6 +440,8 @@ struct smip_stack {
         L.C = C;
         L.err = err;
         L.num_sms = ctx->num_sms;
+        L.scratch = kscratch;
+        L.tile_cnt = ktile_cnt;
         if (timing) {
             if (ev_used == ev_pool.size()) {
                 cudaEvent_t a, b;
@@ -627,6 +637,8 @@ extern "C" int smip_stack_reset(smip_stack_t s)
     CUDA_TRY(cudaMemsetAsync(s->P, 0, sizeof(double) * s->half_elems(), s->st));
     CUDA_TRY(cudaMemsetAsync(s->sum, 0, 8 * s->frame_elems(), s->st));
     CUDA_TRY(cudaMemsetAsync(s->err, 0, sizeof(int), s->st));
+    if (s->ktile_cnt) // a launch that stopped early (timeout) may leave parts counted
+        CUDA_TRY(cudaMemsetAsync(s->ktile_cnt, 0, sizeof(int) * s->ctx->num_sms, s->st));
     s->nframes = 0;
     s->pending = 0;
     s->has_ref = false;
