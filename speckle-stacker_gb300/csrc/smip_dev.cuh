@@ -186,8 +186,42 @@ __device__ __forceinline__ dfc tw_conj(dfc w)
     return w;
 }
 
+// Butterflies with the twiddles 1 and -i (+i for the inverse): no multiply,
+// the product by a unit is a swap and sign change of hi and lo parts.
+__device__ __forceinline__ void bfly_one(float2& a, float2& b)
+{
+    const float2 u = a;
+    a = cadd(u, b);
+    b = csub(u, b);
+}
+__device__ __forceinline__ void bfly_one(dfc& a, dfc& b)
+{
+    const dfc u = a;
+    a = df_cadd(u, b);
+    b = df_csub(u, b);
+}
+__device__ __forceinline__ float2 mul_mi(float2 b, int sign) // b * (-i), or b * (+i) when sign > 0
+{
+    return sign > 0 ? make_float2(-b.y, b.x) : make_float2(b.y, -b.x);
+}
+__device__ __forceinline__ dfc mul_mi(const dfc& b, int sign)
+{
+    dfc r;
+    r.h = mul_mi(b.h, sign);
+    r.l = mul_mi(b.l, sign);
+    return r;
+}
+template <typename C> __device__ __forceinline__ void bfly_mi(C& a, C& b, int sign)
+{
+    C t = mul_mi(b, sign);
+    bfly_one(a, t);
+    b = t;
+}
+
 // Stages s0+1 .. s0+K of an n = 2^logn DIT FFT on nl padded lines (stride ls).
-template <int K, typename C>
+// FIRST (s0 == 0): every twiddle index is known at compile time, and the
+// twiddles 1 and -i (stages 1-3) skip the complex multiply.
+template <int K, typename C, bool FIRST = false>
 __device__ __forceinline__ void fft_pass(C* buf, int logn, int nl, int ls, const C* tw, int twlog, int sign, int s0)
 {
     const int gsh = logn - K; // log2 of the groups per line
@@ -209,10 +243,17 @@ __device__ __forceinline__ void fft_pass(C* buf, int logn, int nl, int ls, const
             for (int m0 = 0; m0 < (1 << K); ++m0) {
                 if (m0 & hm)
                     continue;
-                C w = tw[(((m0 & (hm - 1)) << s0) + j) << tsh];
-                if (sign > 0)
-                    w = tw_conj(w);
-                bfly(v[m0], v[m0 + hm], w);
+                const int k = m0 & (hm - 1); // twiddle exponent within the stage
+                if (FIRST && k == 0) {
+                    bfly_one(v[m0], v[m0 + hm]);                  // w = 1
+                } else if (FIRST && 4 * k == (1 << t)) {
+                    bfly_mi(v[m0], v[m0 + hm], sign);             // w = exp(-i pi/2)
+                } else {
+                    C w = tw[((k << s0) + j) << tsh];
+                    if (sign > 0)
+                        w = tw_conj(w);
+                    bfly(v[m0], v[m0 + hm], w);
+                }
             }
         }
 #pragma unroll
@@ -231,7 +272,14 @@ __device__ void fft_passes(C* buf, int logn, int nl, int ls, const C* tw, int tw
     int s0 = 0;
     for (int p = 0; p < np; ++p) {
         const int k = (logn - s0 + (np - p) - 1) / (np - p);
-        if (k == 3)
+        if (p == 0) {
+            if (k == 3)
+                fft_pass<3, C, true>(buf, logn, nl, ls, tw, twlog, sign, 0);
+            else if (k == 2)
+                fft_pass<2, C, true>(buf, logn, nl, ls, tw, twlog, sign, 0);
+            else
+                fft_pass<1, C, true>(buf, logn, nl, ls, tw, twlog, sign, 0);
+        } else if (k == 3)
             fft_pass<3>(buf, logn, nl, ls, tw, twlog, sign, s0);
         else if (k == 2)
             fft_pass<2>(buf, logn, nl, ls, tw, twlog, sign, s0);

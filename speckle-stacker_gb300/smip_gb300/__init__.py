@@ -169,7 +169,14 @@ class Stack:
     """Device-resident speckle-masking accumulators for one stack of frames."""
 
     def __init__(self, ncols: int, nrows: int, bdepth: int, device: int = 0, stream: int | None = None,
-                 batch_frames: int = 0):
+                 batch_frames=0, dtype=np.uint16):
+        """batch_frames: frames per accumulation batch; 0 = library default,
+        "auto" = the autotuner's cached best for this device and shape (tuned
+        on first use, smip_gb300.autotune); dtype only informs "auto"."""
+        if batch_frames == "auto":
+            from smip_gb300 import autotune
+
+            batch_frames = autotune.best_batch(ncols, nrows, bdepth, dtype, device)
         h = C.c_void_p()
         _check(_L().smip_stack_create(C.byref(h), device, ncols, nrows, bdepth,
                                       C.c_void_p(stream) if stream else None, batch_frames))

@@ -1,0 +1,108 @@
+"""Frame-batch autotuner.
+
+A stack accumulates its frames in batches of ``batch_frames``: every batch is
+one pass of the FFT kernels and one launch of the bispectrum kernel, whose
+packed accumulator (read and written once per launch) and work split (tiles
+per SM, frames per split part) depend on the batch size.  The library's
+default is 64 MB of spectra per batch (240 frames at 256x256, capped at 256).
+This module times candidate batch sizes for a shape on the device at hand,
+keeps the fastest, and caches it per (device, shape, depth, dtype) in a JSON
+file next to the package, so ``Stack(..., batch_frames="auto")`` pays for the
+search once.
+"""
+from __future__ import annotations
+
+import json
+import os
+import threading
+import time
+
+import numpy as np
+
+CACHE = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), ".autotune.json")
+CANDIDATES = (32, 64, 128, 256, 512, 1024)
+_lock = threading.Lock()
+
+
+def _key(device_name: str, ncols: int, nrows: int, bdepth: int, dtype: str) -> str:
+    return f"{device_name}|{ncols}x{nrows}|d{(bdepth // 2) * 2}|{dtype}"
+
+
+def _device_name(device: int) -> str:
+    try:
+        import torch
+
+        return torch.cuda.get_device_name(device)
+    except Exception:  # pragma: no cover - torch without CUDA
+        return f"cuda{device}"
+
+
+def _load() -> dict:
+    try:
+        with open(CACHE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(table: dict):
+    tmp = CACHE + f".{os.getpid()}.tmp"
+    with open(tmp, "w") as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+    os.replace(tmp, CACHE)
+
+
+def spectra_bytes_per_frame(ncols: int, nrows: int) -> int:
+    """Device bytes one batched frame holds (row spectra in float-float,
+    spectra, correlation columns and rows), which bounds the batch size."""
+    hw = ncols // 2 + 1
+    return hw * nrows * (16 + 8 + 8) + ncols * nrows * 4
+
+
+def measure(ncols: int, nrows: int, bdepth: int, batch_frames: int, frames: np.ndarray, device: int = 0,
+            repeats: int = 2) -> float:
+    """frames/s of pushing ``frames`` (already batched in ``batch_frames``)."""
+    from smip_gb300 import Stack
+
+    with Stack(ncols, nrows, bdepth, device=device, batch_frames=batch_frames) as st:
+        st.push_frames(frames)  # warm-up (allocations, first launch)
+        st.sync()
+        best = 0.0
+        for _ in range(repeats):
+            st.reset()
+            t0 = time.perf_counter()
+            st.push_frames(frames)
+            st.flush()
+            st.sync()
+            best = max(best, len(frames) / (time.perf_counter() - t0))
+    return best
+
+
+def tune(ncols: int, nrows: int, bdepth: int, dtype=np.uint16, device: int = 0, candidates=CANDIDATES,
+         mem_limit: float = 8e9, seed: int = 99) -> dict:
+    """Times every candidate batch size (those whose batch buffers fit in
+    ``mem_limit`` bytes) on 2 x the largest candidate's frames of seeded noise;
+    returns {"batch_frames": best, "frames_per_s": {candidate: rate}}."""
+    per = spectra_bytes_per_frame(ncols, nrows)
+    cands = [c for c in candidates if c * per <= mem_limit] or [min(candidates)]
+    n = 2 * max(cands)
+    rng = np.random.default_rng(seed)
+    hi = 255 if np.dtype(dtype) == np.uint8 else 4095
+    frames = rng.integers(0, hi, (n, nrows, ncols)).astype(dtype)
+    rates = {c: measure(ncols, nrows, bdepth, c, frames, device) for c in cands}
+    best = max(rates, key=rates.get)
+    return {"batch_frames": int(best), "frames_per_s": {str(k): v for k, v in rates.items()}}
+
+
+def best_batch(ncols: int, nrows: int, bdepth: int, dtype=np.uint16, device: int = 0) -> int:
+    """The cached best batch size for this device and shape, tuning on first use."""
+    key = _key(_device_name(device), ncols, nrows, bdepth, np.dtype(dtype).name)
+    with _lock:
+        table = _load()
+        if key in table:
+            return int(table[key]["batch_frames"])
+        res = tune(ncols, nrows, bdepth, dtype, device)
+        table = _load()
+        table[key] = res
+        _store(table)
+        return int(res["batch_frames"])

@@ -102,3 +102,47 @@ def test_results_same_alone_and_in_mix(smip):
         assert np.array_equal(r.flags, a.flags)
         assert np.array_equal(r.phases, a.phases)
         assert np.array_equal(r.image, a.image)
+
+
+def test_autotune_cache_roundtrip(tmp_path, monkeypatch):
+    """best_batch tunes once per (device, shape, depth, dtype) and then reads
+    the cache; the measurement itself is replaced by a stand-in here."""
+    from smip_gb300 import autotune
+
+    monkeypatch.setattr(autotune, "CACHE", str(tmp_path / "at.json"))
+    monkeypatch.setattr(autotune, "_device_name", lambda d: "dev")
+    calls = []
+
+    def fake_measure(nc, nr, d, bf, frames, device=0, repeats=2):
+        calls.append(bf)
+        return 1000.0 - abs(bf - 256)  # best at 256
+
+    monkeypatch.setattr(autotune, "measure", fake_measure)
+    assert autotune.best_batch(64, 64, 16, np.uint8) == 256
+    n = len(calls)
+    assert n == len(autotune.CANDIDATES)
+    assert autotune.best_batch(64, 64, 16, np.uint8) == 256 and len(calls) == n  # cached
+    assert autotune.best_batch(64, 64, 17, np.uint8) == 256 and len(calls) == n  # depth 17 acts as 16
+    autotune.best_batch(64, 64, 16, np.uint16)
+    assert len(calls) == 2 * n
+
+
+@pytest.mark.gpu
+def test_autotune_on_device(smip, tmp_path, monkeypatch):
+    """A real (small) tuning run picks one of the candidates and the stack it
+    configures gives the same bispectrum as the default batch size."""
+    from smip_gb300 import autotune
+
+    monkeypatch.setattr(autotune, "CACHE", str(tmp_path / "at.json"))
+    monkeypatch.setattr(autotune, "CANDIDATES", (16, 32, 64))
+    bf = autotune.best_batch(32, 32, 8, np.uint8)
+    assert bf in (16, 32, 64)
+    rng = np.random.default_rng(3)
+    frames = rng.integers(0, 255, (40, 32, 32)).astype(np.uint8)
+    with smip.Stack(32, 32, 8, batch_frames="auto", dtype=np.uint8) as a, smip.Stack(32, 32, 8) as b:
+        a.push_frames(frames)
+        b.push_frames(frames)
+        assert np.array_equal(a.shifts(), b.shifts())
+        from conftest import rel_l2
+
+        assert rel_l2(a.bispectrum(), b.bispectrum()) <= 1e-6
