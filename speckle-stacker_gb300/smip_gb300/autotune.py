@@ -78,11 +78,12 @@ def measure(ncols: int, nrows: int, bdepth: int, batch_frames: int, frames: np.n
     return best
 
 
-def tune(ncols: int, nrows: int, bdepth: int, dtype=np.uint16, device: int = 0, candidates=CANDIDATES,
+def tune(ncols: int, nrows: int, bdepth: int, dtype=np.uint16, device: int = 0, candidates=None,
          mem_limit: float = 8e9, seed: int = 99) -> dict:
     """Times every candidate batch size (those whose batch buffers fit in
     ``mem_limit`` bytes) on 2 x the largest candidate's frames of seeded noise;
     returns {"batch_frames": best, "frames_per_s": {candidate: rate}}."""
+    candidates = CANDIDATES if candidates is None else candidates
     per = spectra_bytes_per_frame(ncols, nrows)
     cands = [c for c in candidates if c * per <= mem_limit] or [min(candidates)]
     n = 2 * max(cands)
