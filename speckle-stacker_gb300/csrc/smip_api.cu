@@ -506,9 +506,14 @@ extern "C" int smip_stack_create(smip_stack_t* out, int device, long ncols, long
     s->g = g;
     s->bdepth_req = bdepth;
     if (batch_frames <= 0) {
-        const size_t per = sizeof(float2) * (size_t)g.hw * g.H;
-        long bf = (long)((64ull << 20) / per);
-        batch_frames = std::min<long>(256, std::max<long>(16, bf / 16 * 16));
+        // ~2 GB of per-batch buffers (float-float row spectra, spectra,
+        // correlation columns and rows, frames), at most 1024 frames: larger
+        // batches amortise the bispectrum's read-modify-write and split the
+        // bispectrum kernel's work more evenly (measured by the autotuner:
+        // 1024 beats 256 by 5 % at 256x256, 13 % at 128x128, 36 % at 64x64)
+        const size_t per = (size_t)g.hw * g.H * (sizeof(dfc) + 2 * sizeof(float2)) + (size_t)g.W * g.H * (4 + 8);
+        const long bf = (long)((2ull << 30) / per);
+        batch_frames = std::min<long>(1024, std::max<long>(16, bf / 16 * 16));
     }
     s->Bf = (int)batch_frames;
     if (stream) {

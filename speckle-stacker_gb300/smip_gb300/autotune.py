@@ -4,7 +4,7 @@ A stack accumulates its frames in batches of ``batch_frames``: every batch is
 one pass of the FFT kernels and one launch of the bispectrum kernel, whose
 packed accumulator (read and written once per launch) and work split (tiles
 per SM, frames per split part) depend on the batch size.  The library's
-default is 64 MB of spectra per batch (240 frames at 256x256, capped at 256).
+default is about 2 GB of batch buffers (1024 frames at 256x256 and below).
 This module times candidate batch sizes for a shape on the device at hand,
 keeps the fastest, and caches it per (device, shape, depth, dtype) in a JSON
 file next to the package, so ``Stack(..., batch_frames="auto")`` pays for the
