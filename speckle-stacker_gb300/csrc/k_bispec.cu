@@ -15,7 +15,10 @@
 // of JT = 32 * NJB consecutive j:
 //   main tile  (a0, j tile, chunk): rows a2 = 1..d/2 in chunks of RPC rows;
 //   row-0 tile (a0 group, j tile):  row a2 = 0 for RPC consecutive a0.
-// Warp w takes j block w % NJB and (l block, row) from w / NJB.
+// Warp w takes j block w % NJB and (l block, row) from w / NJB.  The grid has
+// one CTA per tile, so the block scheduler places tiles on whichever SMs are
+// free; the tiles of the last partial wave are split by frames into parts
+// (one CTA each) whose partial sums are merged by the tile's last part.
 //
 //   lane (jg, lg) -> j = jw + jg + 4 a (a < 8),  l = -d/2 + 8 TLW lb + lg + 8 b (b < TLW)
 //   every lane    -> also the l = +d/2 column for j = jw + lane (last l block)
@@ -90,13 +93,13 @@ struct BispecArgs {
     int njt;      // j tiles: ceil(H / JT)
     int nmain;    // main tiles
     int ntiles;   // main + row-0 tiles
-    // Work split (stream-K style): every CTA runs R whole tiles b + k*G; the
-    // last ntiles - R*G tiles are split by frames into P parts each, one part
-    // per CTA b < nsplit.  Parts write partial sums to scratch; the CTA that
+    // Work units, one CTA each: tiles [0, nfull) whole; the remaining tiles
+    // (a last partial wave of the GPU) split by frames into P parts each
+    // (nsplit units).  Parts write partial sums to scratch; the CTA that
     // completes a tile's last part adds the parts, in part order, into (B, C).
-    int G, R, P, nsplit;
+    int nfull, P, nsplit;
     float2* scratch;   // [nsplit][NSLOT][THREADS] partial sums
-    int* tile_cnt;     // [ntiles - R*G] parts finished (zero between launches)
+    int* tile_cnt;     // [ntiles - nfull] parts finished (zero between launches)
 };
 
 // Tile geometry shared by the TMA issue path and the consumers.
@@ -161,30 +164,22 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
     __syncthreads();
     const int half_h = p.H / 2;
     const int nf = p.nframes;
-    // this CTA's units: R whole tiles b + k*G, then (if b < nsplit) part
-    // b % P of split tile R*G + b / P, frames [part*nf/P, (part+1)*nf/P)
-    auto split_tile = [&]() { return p.R * p.G + (int)blockIdx.x / p.P; };
-    auto split_f0 = [&]() { return (int)((long long)((int)blockIdx.x % p.P) * nf / p.P); };
-    auto split_f1 = [&]() { return (int)((long long)((int)blockIdx.x % p.P + 1) * nf / p.P); };
-    const bool has_split = (int)blockIdx.x < p.nsplit;
-    const int my_units = p.R + (has_split ? 1 : 0);
-    const uint32_t total = (uint32_t)p.R * (uint32_t)nf + (has_split ? (uint32_t)(split_f1() - split_f0()) : 0u);
+    // this CTA's unit: tile blockIdx.x whole, or (split unit s = blockIdx.x -
+    // nfull) part s % P of tile nfull + s / P, frames [part*nf/P, (part+1)*nf/P)
+    const bool split_unit = (int)blockIdx.x >= p.nfull;
+    auto split_s = [&]() { return (int)blockIdx.x - p.nfull; };
+    auto split_tile = [&]() { return p.nfull + split_s() / p.P; };
+    auto split_f0 = [&]() { return (int)((long long)(split_s() % p.P) * nf / p.P); };
+    auto split_f1 = [&]() { return (int)((long long)(split_s() % p.P + 1) * nf / p.P); };
+    const uint32_t total = split_unit ? (uint32_t)(split_f1() - split_f0()) : (uint32_t)nf;
     const int cv = (half_h - DE / 2) & ~1;
     const int offv = (half_h - DE / 2) - cv;
 
     // issue the loads of iteration r (tile r / nframes, frame r % nframes) into stage r % NS;
     // box x coordinates are in 8-byte elements and even (16-byte aligned)
     auto issue = [&](uint32_t r) {
-        int f, t;
-        const uint32_t full_iters = (uint32_t)p.R * (uint32_t)nf;
-        if (r < full_iters) {
-            const uint32_t k = r / nf;
-            f = (int)(r - k * nf);
-            t = (int)blockIdx.x + (int)k * p.G;
-        } else {
-            f = split_f0() + (int)(r - full_iters);
-            t = split_tile();
-        }
+        const int f = split_unit ? split_f0() + (int)r : (int)r;
+        const int t = split_unit ? split_tile() : (int)blockIdx.x;
         const TileInfo ti = decode_tile<DE>(t, p);
         const int cw = (ti.j0 + half_h - DE / 2) & ~1;
         const int s = r % Cf::NS;
@@ -223,10 +218,9 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
     uint32_t r = 0;
     bool ok = true;
     __shared__ int s_last; // this CTA completes its split tile
-    for (int k = 0; k < my_units && ok; ++k) {
-        const bool split_unit = k == p.R;       // the part of a split tile
-        const int nfu = split_unit ? split_f1() - split_f0() : nf; // frames of this unit
-        const TileInfo ti = decode_tile<DE>(split_unit ? split_tile() : (int)blockIdx.x + k * p.G, p);
+    for (int k = 0; k < 1 && ok; ++k) {
+        const int nfu = (int)total; // frames of this unit
+        const TileInfo ti = decode_tile<DE>(split_unit ? split_tile() : (int)blockIdx.x, p);
         const int a0 = ti.row0 ? ti.a0 + wr : ti.a0;
         const int a2 = ti.row0 ? 0 : 1 + ti.c * Cf::RPC + wr;
         const int vrow = ti.row0 ? 0 : wr;
@@ -312,7 +306,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
         if (split_unit && p.P > 1) {
             // write this part's sums; the CTA that finishes the tile's last part merges
             constexpr int NSLOT = 8 * Cf::TLW + 1;
-            const int b = (int)blockIdx.x, s_part = b % p.P, s_tile = split_tile();
+            const int b = split_s(), s_part = b % p.P, s_tile = split_tile();
             float2* sc = p.scratch + (long long)b * NSLOT * Cf::THREADS + threadIdx.x;
 #pragma unroll
             for (int a = 0; a < 8; ++a)
@@ -323,7 +317,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
             __threadfence();
             __syncthreads();
             if (threadIdx.x == 0)
-                s_last = atomicAdd(&p.tile_cnt[s_tile - p.R * p.G], 1) == p.P - 1;
+                s_last = atomicAdd(&p.tile_cnt[s_tile - p.nfull], 1) == p.P - 1;
             __syncthreads();
             if (!s_last)
                 continue;
@@ -351,7 +345,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
                 acce.y += v.y;
             }
             if (threadIdx.x == 0)
-                p.tile_cnt[s_tile - p.R * p.G] = 0; // ready for the next launch
+                p.tile_cnt[s_tile - p.nfull] = 0; // ready for the next launch
         }
         const int D = EXACT ? DE : p.D;
         const int hd = D / 2; // a depth below DE computes the template's extra rows and columns, stores none
@@ -487,22 +481,24 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
     a.njt = (g.H + Cf::JT - 1) / Cf::JT;
     a.nmain = g.hw * a.njt * a.nchm;
     a.ntiles = a.nmain + (g.hw + Cf::RPC - 1) / Cf::RPC * a.njt;
-    // Whole rounds of G tiles, then the remainder split by frames so that every
-    // CTA gets the same work (parts of at least 8 frames).
-    a.G = L.num_sms;
-    a.R = a.ntiles / a.G;
-    const int rem = a.ntiles - a.R * a.G;
-    int P = rem > 0 ? a.G / rem : 1;
+    // One CTA per unit (not persistent, so the block scheduler can place tiles
+    // on whichever SMs are free, also while other streams' kernels run).  The
+    // tiles of the last partial wave (one CTA per SM) are split by frames so
+    // that the wave is full (parts of at least 8 frames).
+    const int G = L.num_sms;
+    const int rem = a.ntiles % G;
+    int P = rem > 0 ? G / rem : 1;
     P = P < 1 ? 1 : P;
     const int pmax = L.nframes / 8 > 1 ? L.nframes / 8 : 1;
     P = P > pmax ? pmax : P;
     if (!L.scratch || !L.tile_cnt)
         P = 1;
+    a.nfull = a.ntiles - (P > 1 ? rem : 0);
     a.P = P;
-    a.nsplit = rem * P;
+    a.nsplit = P > 1 ? rem * P : 0;
     a.scratch = L.scratch;
     a.tile_cnt = L.tile_cnt;
-    const int grid = a.R > 0 ? a.G : a.nsplit;
+    const int grid = a.nfull + a.nsplit;
     bispec_accum_kernel<DE, EXACT><<<grid, Cf::THREADS, Cf::SMEM, st>>>(mW, mV, mA, a); note_launches(1);
     return cudaGetLastError();
 }
