@@ -238,8 +238,11 @@ def serving_metrics(jobs):
         eng = serve.Engine(budget_bytes=120e9, max_active=64, workers=32)
         eng.prewarm(shapes, count=24)
         serve.run_plain(jl[:3], realtime=False)  # warm the code paths
-        res_s, span_s = eng.run(jl, realtime=realtime)
-        res_p, span_p = serve.run_plain(jl, realtime=realtime)
+        # best of two runs of each (host thread scheduling varies run to run)
+        runs_s = [eng.run(jl, realtime=realtime) for _ in range(2)]
+        runs_p = [serve.run_plain(jl, realtime=realtime) for _ in range(2)]
+        res_s, span_s = min(runs_s, key=lambda x: x[1])
+        res_p, span_p = min(runs_p, key=lambda x: x[1])
         s, p = serve.summarize(res_s, span_s), serve.summarize(res_p, span_p)
         out[key] = {"workload": desc, "served": s, "plain": p,
                     "frames_per_s_ratio": s["frames_per_s"] / p["frames_per_s"],

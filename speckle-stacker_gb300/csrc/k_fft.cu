@@ -14,8 +14,9 @@
 // energy -- carries FP32 relative accuracy, as the reference's FP64 FFT
 // narrowed to complex<float> (bispectrum.h:399) does.  A plain FP32 FFT loses
 // up to 1e-2 relative accuracy in such bins and 5e-2 in bispectrum elements
-// that are cancellations of them.  The power spectrum is formed from the
-// float-float values in FP64.  The correlation's inverse transform only
+// that are cancellations of them.  The power spectrum is |F|^2 of the
+// float-float values, summed over a chunk's frames in float-float and over
+// chunks in FP64.  The correlation's inverse transform only
 // locates the peak (candidates are re-scored exactly, k_xcorr.cu) and stays
 // FP32.
 //
@@ -93,7 +94,7 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const T* __restrict__ fra
 
 // ------------------------------------------------------------- column pass
 // One CTA per (a, chunk of frames).  Float-float forward FFT along y gives
-// Fm(a, y) = F(-a, y); writes S (rounded to FP32), accumulates |F|^2 in FP64
+// Fm(a, y) = F(-a, y); writes S (rounded to FP32), accumulates |F|^2 in float-float
 // (frame order), and for the correlation computes the FP32 inverse
 // y-transform of conj(R) * Fm into T.
 __global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __restrict__ Gt, float2* __restrict__ S,
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __re
     float2* tw = reinterpret_cast<float2*>(L1 + kColLines * LH);   // 2^(kTwLog-1)
     float2* R = tw + (1 << (kTwLog - 1));                          // [H]
     float2* L2 = R + H;                                            // [kColLines][LH]
-    double* pacc = reinterpret_cast<double*>(L2 + kColLines * LH); // [H]
+    float2* pacc = reinterpret_cast<float2*>(L2 + kColLines * LH); // [H] float-float (hi, lo)
     const int a = blockIdx.x;
     const int chunk = blockIdx.y;
     const int fbeg = chunk * fpc;
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __re
     if (mode == 0)
         for (int y = threadIdx.x; y < H; y += blockDim.x) {
             R[y] = Rbuf[(long long)a * H + y];
-            pacc[y] = 0.0;
+            pacc[y] = make_float2(0.f, 0.f);
         }
     for (int f0 = fbeg; f0 < fend; f0 += kColLines) {
         const int nl = min(kColLines, fend - f0);
@@ -141,15 +142,20 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __re
             const int l = idx >> logH, c = idx & (H - 1);
             S[(f0 + l) * gstride + (long long)a * H + c] = df_round(L1[l * LH + pad8((c + H / 2) & (H - 1))]);
         }
-        // power spectrum, frames in order per element, from the float-float values
+        // power spectrum, frames in order per element: |F|^2 of the float-float values
+        // summed in float-float (~48-bit) on the FP32 pipes; GB300's FP64 rate is
+        // too low for this per-element sum
         for (int c = threadIdx.x; c < H; c += blockDim.x) {
-            double acc = pacc[c];
+            float ah = pacc[c].x, al = pacc[c].y;
             for (int l = 0; l < nl; ++l) {
                 const dfc v = L1[l * LH + pad8((c + H / 2) & (H - 1))];
-                const double re = (double)v.h.x + (double)v.l.x, im = (double)v.h.y + (double)v.l.y;
-                acc += re * re + im * im;
+                float rh, rl, ih, il, sh, sl;
+                df_mul(v.h.x, v.l.x, v.h.x, v.l.x, rh, rl);
+                df_mul(v.h.y, v.l.y, v.h.y, v.l.y, ih, il);
+                df_add(rh, rl, ih, il, sh, sl);
+                df_add(ah, al, sh, sl, ah, al);
             }
-            pacc[c] = acc;
+            pacc[c] = make_float2(ah, al);
         }
         // correlation product conj(R) * F in FP32, bit-reversed for the inverse FFT
         for (int idx = threadIdx.x; idx < nl * H; idx += blockDim.x) {
@@ -168,7 +174,7 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __re
     }
     __syncthreads();
     for (int c = threadIdx.x; c < H; c += blockDim.x)
-        Ppart[(long long)chunk * gstride + (long long)a * H + c] = pacc[c];
+        Ppart[(long long)chunk * gstride + (long long)a * H + c] = (double)pacc[c].x + (double)pacc[c].y;
 }
 
 __global__ void power_reduce_kernel(double* __restrict__ P, const double* __restrict__ Ppart, int nchunks, long long n)
