@@ -272,26 +272,32 @@ __device__ __forceinline__ double abs_px(double v) { return fabs(v); }
 // sum[y][x] += |frame[y + sy][x + sx]| where inside the frame, frames in
 // order (main.cpp:293-294); the stack's frame 0 enters unshifted with its
 // sign (main.cpp:266).
+// Integer frames (u64 sums) are exact in any order, so the batch's frames are
+// also split over gridDim.y CTAs whose partial sums are added atomically;
+// float frames (f64 sums) keep one CTA per pixel block, frames in order.
 template <typename T, typename A>
 __global__ void __launch_bounds__(256) saa_add_kernel(A* __restrict__ sum, const T* __restrict__ frames,
                                                       long long fstride, int nframes, int first_is_frame0,
                                                       const int* __restrict__ shifts, int W, int H)
 {
-    extern __shared__ int2 sh[]; // the batch's shifts
-    for (int f = threadIdx.x; f < nframes; f += blockDim.x)
-        sh[f] = make_int2(shifts[2 * f], shifts[2 * f + 1]);
+    extern __shared__ int2 sh[]; // this CTA's frames' shifts
+    constexpr bool kExact = sizeof(A) == 8 && A(-1) > A(0); // unsigned 64-bit sum
+    const int fb = (int)((long long)blockIdx.y * nframes / gridDim.y);
+    const int fe = (int)((long long)(blockIdx.y + 1) * nframes / gridDim.y);
+    for (int f = fb + threadIdx.x; f < fe; f += blockDim.x)
+        sh[f - fb] = make_int2(shifts[2 * f], shifts[2 * f + 1]);
     __syncthreads();
     const int n = W * H;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const int x = p & (W - 1), y = p / W;
-        A acc = sum[p];
-        int f = 0;
-        for (; f + 8 <= nframes; f += 8) { // eight independent loads in flight, added in frame order
+        A acc = kExact ? A(0) : sum[p];
+        int f = fb;
+        for (; f + 8 <= fe; f += 8) { // eight independent loads in flight, added in frame order
             A v[8];
             bool in[8];
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
-                const int xs = x + sh[f + q].x, ys = y + sh[f + q].y;
+                const int xs = x + sh[f - fb + q].x, ys = y + sh[f - fb + q].y;
                 in[q] = xs >= 0 && xs < W && ys >= 0 && ys < H;
                 v[q] = in[q] ? (A)frames[(long long)(f + q) * fstride + ys * W + xs] : (A)0;
             }
@@ -300,14 +306,17 @@ __global__ void __launch_bounds__(256) saa_add_kernel(A* __restrict__ sum, const
                 if (in[q])
                     acc += (first_is_frame0 && f + q == 0) ? v[q] : abs_px(v[q]);
         }
-        for (; f < nframes; ++f) {
-            const int xs = x + sh[f].x, ys = y + sh[f].y;
+        for (; f < fe; ++f) {
+            const int xs = x + sh[f - fb].x, ys = y + sh[f - fb].y;
             if (xs >= 0 && xs < W && ys >= 0 && ys < H) {
                 const A v = (A)frames[(long long)f * fstride + ys * W + xs];
                 acc += (first_is_frame0 && f == 0) ? v : abs_px(v);
             }
         }
-        sum[p] = acc;
+        if constexpr (kExact)
+            atomicAdd(reinterpret_cast<unsigned long long*>(&sum[p]), (unsigned long long)acc);
+        else
+            sum[p] = acc;
     }
 }
 
@@ -342,8 +351,18 @@ cudaError_t launch_saa_add(int dtype, void* sum, const void* frames, long long f
                            int first_is_frame0, const int* shifts, const Geometry& g, cudaStream_t st)
 {
     const int n = g.W * g.H;
-    const int grid = (n + 255) / 256;
-    const size_t shm = sizeof(int2) * (size_t)(nframes > 0 ? nframes : 1);
+    const int gx = (n + 255) / 256;
+    // integer frames: frame groups of >= 32 frames, enough CTAs to fill a
+    // 152-SM GPU about four deep
+    constexpr int kTargetCtas = 4 * 152;
+    int gy = 1;
+    if (dtype <= 1) {
+        gy = (kTargetCtas + gx - 1) / gx;
+        gy = gy > nframes / 32 ? nframes / 32 : gy;
+        gy = gy < 1 ? 1 : gy;
+    }
+    const dim3 grid(gx, dtype <= 1 ? gy : 1);
+    const size_t shm = sizeof(int2) * (size_t)(nframes > 0 ? (nframes + grid.y - 1) / grid.y + 1 : 1);
     switch (dtype) {
     case 0: saa_add_kernel<uint8_t, unsigned long long><<<grid, 256, shm, st>>>((unsigned long long*)sum, (const uint8_t*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
     case 1: saa_add_kernel<uint16_t, unsigned long long><<<grid, 256, shm, st>>>((unsigned long long*)sum, (const uint16_t*)frames, fstride, nframes, first_is_frame0, shifts, g.W, g.H); note_launches(1); break;
