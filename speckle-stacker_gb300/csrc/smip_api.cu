@@ -317,7 +317,14 @@ struct smip_stack {
     double* P = nullptr;
     double* Ppart = nullptr;
     void* sum = nullptr;          // u64 (integer frames) or double
-    void* staging = nullptr;      // Bf raw frames
+    // Two frame batches: the host->device (or device->device) copy of the next
+    // batch runs on the copy stream cst while the kernels read the current one.
+    void* stg[2] = { nullptr, nullptr };
+    int cur = 0;                  // buffer being filled
+    cudaStream_t cst = nullptr;   // copy stream
+    cudaEvent_t ev_copied[2] = { nullptr, nullptr }; // copies into stg[i] done (on cst)
+    cudaEvent_t ev_free[2] = { nullptr, nullptr };   // kernels done reading stg[i] (on st)
+    bool free_rec[2] = { false, false };
     double* spec_staging = nullptr; // spectra input (mode 2)
     void* ref = nullptr;          // raw frame 0
     double* ref_sq = nullptr;
@@ -341,7 +348,15 @@ struct smip_stack {
             cudaStreamSynchronize(st);
         dfree(B); dfree(C); dfree(Bn); dfree(P); dfree(Ppart);
         if (sum) cudaFree(sum);
-        if (staging) cudaFree(staging);
+        if (cst)
+            cudaStreamSynchronize(cst);
+        for (int i = 0; i < 2; ++i) {
+            if (stg[i]) cudaFree(stg[i]);
+            if (ev_copied[i]) cudaEventDestroy(ev_copied[i]);
+            if (ev_free[i]) cudaEventDestroy(ev_free[i]);
+        }
+        if (cst)
+            cudaStreamDestroy(cst);
         dfree(spec_staging);
         if (ref) cudaFree(ref);
         dfree(ref_sq); dfree(Gt); dfree(T); dfree(S); dfree(R); dfree(corr); dfree(shifts); dfree(err);
@@ -398,6 +413,35 @@ struct smip_stack {
         return SMIP_OK;
     }
 
+    // the two frame buffers, the copy stream and its events (first frames)
+    int ensure_staging(size_t fbytes)
+    {
+        if (!cst)
+            CUDA_TRY(cudaStreamCreateWithFlags(&cst, cudaStreamNonBlocking));
+        for (int i = 0; i < 2; ++i) {
+            if (!stg[i])
+                CUDA_TRY(cudaMalloc(&stg[i], fbytes * Bf));
+            if (!ev_copied[i])
+                CUDA_TRY(cudaEventCreateWithFlags(&ev_copied[i], cudaEventDisableTiming));
+            if (!ev_free[i])
+                CUDA_TRY(cudaEventCreateWithFlags(&ev_free[i], cudaEventDisableTiming));
+        }
+        return SMIP_OK;
+    }
+
+    void free_staging()
+    {
+        if (cst)
+            cudaStreamSynchronize(cst);
+        for (int i = 0; i < 2; ++i) {
+            if (stg[i])
+                cudaFree(stg[i]);
+            stg[i] = nullptr;
+            free_rec[i] = false;
+        }
+        cur = 0;
+    }
+
     int run_batch()
     {
         const int n = pending;
@@ -409,6 +453,10 @@ struct smip_stack {
         } else {
             const size_t fe = frame_elems();
             const bool first = !has_ref;
+            void* staging = stg[cur];
+            // the batch's frames are on the copy stream
+            CUDA_TRY(cudaEventRecord(ev_copied[cur], cst));
+            CUDA_TRY(cudaStreamWaitEvent(st, ev_copied[cur], 0));
             int rc = ensure_shift_cap(nframes);
             if (rc)
                 return rc;
@@ -426,6 +474,10 @@ struct smip_stack {
             CUDA_TRY(launch_xcorr_shift(dtype, corr, staging, (long long)fe, ref, ref_sq, n, first ? 1 : 0, g,
                                         shifts + 2 * first_index, st));
             CUDA_TRY(launch_saa_add(dtype, sum, staging, (long long)fe, n, first ? 1 : 0, shifts + 2 * first_index, g, st));
+            // the last reader of this buffer; the copy stream refills it after this
+            CUDA_TRY(cudaEventRecord(ev_free[cur], st));
+            free_rec[cur] = true;
+            cur ^= 1;
             has_ref = true;
         }
         if (!kscratch) {
@@ -559,9 +611,9 @@ extern "C" int smip_stack_push_frames(smip_stack_t s, const void* frames, int dt
         if (s->nframes != 0)
             return fail(SMIP_E_INVALID_ARGUMENT, "frame dtype differs from the stack's first frames");
         CUDA_TRY(cudaStreamSynchronize(s->st)); // after a reset: new element type
-        cudaFree(s->staging);
+        s->free_staging();
         cudaFree(s->ref);
-        s->staging = s->ref = nullptr;
+        s->ref = nullptr;
         s->dtype = -1;
     }
     const size_t fbytes = es * s->frame_elems();
@@ -570,7 +622,8 @@ extern "C" int smip_stack_push_frames(smip_stack_t s, const void* frames, int dt
     if ((size_t)stride_bytes < fbytes)
         return fail(SMIP_E_INVALID_ARGUMENT, "frame stride smaller than a frame");
     if (s->dtype < 0) {
-        CUDA_TRY(cudaMalloc(&s->staging, fbytes * s->Bf));
+        if ((rc = s->ensure_staging(fbytes)))
+            return rc;
         CUDA_TRY(cudaMalloc(&s->ref, fbytes));
         s->dtype = dtype;
     }
@@ -580,11 +633,13 @@ extern "C" int smip_stack_push_frames(smip_stack_t s, const void* frames, int dt
     long done = 0;
     while (done < count) {
         const long k = std::min<long>(count - done, s->Bf - s->pending);
-        char* dst = static_cast<char*>(s->staging) + fbytes * s->pending;
+        if (s->pending == 0 && s->free_rec[s->cur]) // the kernels of the buffer's last batch are done with it
+            CUDA_TRY(cudaStreamWaitEvent(s->cst, s->ev_free[s->cur], 0));
+        char* dst = static_cast<char*>(s->stg[s->cur]) + fbytes * s->pending;
         if ((size_t)stride_bytes == fbytes)
-            CUDA_TRY(cudaMemcpyAsync(dst, src + done * stride_bytes, fbytes * k, kind, s->st));
+            CUDA_TRY(cudaMemcpyAsync(dst, src + done * stride_bytes, fbytes * k, kind, s->cst));
         else
-            CUDA_TRY(cudaMemcpy2DAsync(dst, fbytes, src + done * stride_bytes, stride_bytes, fbytes, k, kind, s->st));
+            CUDA_TRY(cudaMemcpy2DAsync(dst, fbytes, src + done * stride_bytes, stride_bytes, fbytes, k, kind, s->cst));
         s->pending += (int)k;
         s->nframes += k;
         done += k;
@@ -634,6 +689,8 @@ extern "C" int smip_stack_reset(smip_stack_t s)
     if (rc)
         return rc;
     CUDA_TRY(cudaStreamSynchronize(s->st));
+    if (s->cst) // frames copied for a batch that the reset drops
+        CUDA_TRY(cudaStreamSynchronize(s->cst));
     if ((rc = s->collect_timing()))
         return rc;
     const size_t bs = (size_t)s->g.base_size;
@@ -854,10 +911,18 @@ extern "C" int smip_stack_share_reference(smip_stack_t dst, smip_stack_t src)
     if (src->nframes != 0)
         return fail(SMIP_E_BAD_CALL, "src already holds frames");
     const size_t fbytes = dtype_size(dst->dtype) * dst->frame_elems();
+    if (src->dtype >= 0 && src->dtype != dst->dtype) { // buffers sized for another element type
+        CUDA_TRY(cudaStreamSynchronize(src->st));
+        src->free_staging();
+        cudaFree(src->ref);
+        src->ref = nullptr;
+    }
     src->dtype = dst->dtype;
     src->mode = 1;
-    CUDA_TRY(cudaMalloc(&src->staging, fbytes * src->Bf));
-    CUDA_TRY(cudaMalloc(&src->ref, fbytes));
+    if (int rc2 = src->ensure_staging(fbytes))
+        return rc2;
+    if (!src->ref)
+        CUDA_TRY(cudaMalloc(&src->ref, fbytes));
     CUDA_TRY(cudaMemcpy(src->ref, dst->ref, fbytes, cudaMemcpyDeviceToDevice));
     CUDA_TRY(cudaMemcpy(src->R, dst->R, sizeof(float2) * dst->half_elems(), cudaMemcpyDeviceToDevice));
     CUDA_TRY(cudaMemcpy(src->ref_sq, dst->ref_sq, sizeof(double), cudaMemcpyDeviceToDevice));
