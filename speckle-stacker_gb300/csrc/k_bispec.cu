@@ -47,6 +47,8 @@
 // across batches into (B, C) in HBM.  Every mbarrier wait is bounded.
 #include <cuda.h>
 
+#include <algorithm>
+
 #include "smip_dev.cuh"
 
 namespace smip_gpu {
@@ -91,6 +93,10 @@ struct BispecArgs {
     int D;        // the stack's depth (even, <= DE): packed layout and stored elements
     int nchm;     // main chunks per (a0, j tile): ceil((D/2) / RPC)
     int njt;      // j tiles: ceil(H / JT)
+    // Main tiles list only chunks whose first row has u + v inside the
+    // spectrum (a0 + a2 <= hw - 1); the others would add nothing but zeros.
+    // a0 < areg: all nchm chunks (nreg tiles); a0 in [areg, hw - 2]: fewer.
+    int areg, nreg;
     int nmain;    // main tiles
     int ntiles;   // main + row-0 tiles
     // Work units, one CTA each: tiles [0, nfull) whole; the remaining tiles
@@ -110,6 +116,16 @@ struct TileInfo {
     int c;    // main: chunk
 };
 
+// Chunks c of a0 whose first row a2 = 1 + c RPC keeps a0 + a2 <= hw - 1.
+template <int DE>
+__host__ __device__ inline int main_chunks(int a0, int hw, int nchm)
+{
+    if (a0 > hw - 2)
+        return 0;
+    const int nc = (hw - 2 - a0) / BCfg<DE>::RPC + 1;
+    return nc < nchm ? nc : nchm;
+}
+
 template <int DE>
 __device__ __forceinline__ TileInfo decode_tile(int t, const BispecArgs& p)
 {
@@ -117,11 +133,24 @@ __device__ __forceinline__ TileInfo decode_tile(int t, const BispecArgs& p)
     TileInfo ti;
     ti.row0 = t >= p.nmain;
     int jt;
-    if (!ti.row0) {
+    if (!ti.row0 && t < p.nreg) {
         ti.c = t % p.nchm;
         const int rest = t / p.nchm;
         jt = rest % p.njt;
         ti.a0 = rest / p.njt;
+    } else if (!ti.row0) { // the last a0 rows: chunks [0, main_chunks(a0)) each
+        int u = t - p.nreg, a0 = p.areg;
+        for (;;) {
+            const int nc = main_chunks<DE>(a0, p.hw, p.nchm);
+            if (u < nc * p.njt) {
+                jt = u / nc;
+                ti.c = u % nc;
+                break;
+            }
+            u -= nc * p.njt;
+            ++a0;
+        }
+        ti.a0 = a0;
     } else {
         const int t0 = t - p.nmain;
         ti.c = 0;
@@ -175,24 +204,24 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
     const int cv = (half_h - DE / 2) & ~1;
     const int offv = (half_h - DE / 2) - cv;
 
-    // issue the loads of iteration r (tile r / nframes, frame r % nframes) into stage r % NS;
-    // box x coordinates are in 8-byte elements and even (16-byte aligned)
+    // box coordinates of this CTA's tile, set once by thread 0 (x in 8-byte
+    // elements, even: 16-byte aligned); iteration r loads frame f0 + r
+    __shared__ int s_box[7]; // W x, W y, V y, A x, A y, f0, row-0 tile
+
+    // issue the loads of iteration r into stage r % NS
     auto issue = [&](uint32_t r) {
-        const int f = split_unit ? split_f0() + (int)r : (int)r;
-        const int t = split_unit ? split_tile() : (int)blockIdx.x;
-        const TileInfo ti = decode_tile<DE>(t, p);
-        const int cw = (ti.j0 + half_h - DE / 2) & ~1;
+        const int f = s_box[5] + (int)r;
         const int s = r % Cf::NS;
         unsigned char* st = smem + s * Cf::STAGE;
-        if (!ti.row0) {
+        if (!s_box[6]) {
             mbar_arrive_expect_tx(&full[s], Cf::WBYTES + Cf::VBYTES + Cf::ABYTES);
-            tma_load_3d(st + Cf::WOFF, &tmW, cw, ti.a0 + 1 + ti.c * Cf::RPC, f, &full[s]);
-            tma_load_3d(st + Cf::VOFF, &tmV, cv, 1 + ti.c * Cf::RPC, f, &full[s]);
-            tma_load_3d(st + Cf::AOFF, &tmA, ti.j0 + half_h, ti.a0, f, &full[s]);
+            tma_load_3d(st + Cf::WOFF, &tmW, s_box[0], s_box[1], f, &full[s]);
+            tma_load_3d(st + Cf::VOFF, &tmV, cv, s_box[2], f, &full[s]);
+            tma_load_3d(st + Cf::AOFF, &tmA, s_box[3], s_box[4], f, &full[s]);
         } else {
             mbar_arrive_expect_tx(&full[s], Cf::WBYTES + Cf::VBYTES);
-            tma_load_3d(st + Cf::WOFF, &tmW, cw, ti.a0, f, &full[s]);
-            tma_load_3d(st + Cf::VOFF, &tmV, cv, 0, f, &full[s]);
+            tma_load_3d(st + Cf::WOFF, &tmW, s_box[0], s_box[1], f, &full[s]);
+            tma_load_3d(st + Cf::VOFF, &tmV, cv, s_box[2], f, &full[s]);
         }
     };
 
@@ -200,6 +229,14 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
     // that finishes iteration r with r % WARPS == warp issues r + NS - kLag.
     constexpr uint32_t kAhead = Cf::NS - kLag;
     if (threadIdx.x == 0) {
+        const TileInfo ti = decode_tile<DE>(split_unit ? split_tile() : (int)blockIdx.x, p);
+        s_box[0] = (ti.j0 + half_h - DE / 2) & ~1;
+        s_box[1] = ti.row0 ? ti.a0 : ti.a0 + 1 + ti.c * Cf::RPC;
+        s_box[2] = ti.row0 ? 0 : 1 + ti.c * Cf::RPC;
+        s_box[3] = ti.j0 + half_h;
+        s_box[4] = ti.a0;
+        s_box[5] = split_unit ? split_f0() : 0;
+        s_box[6] = ti.row0;
         const uint32_t n0 = total < kAhead ? total : kAhead;
         for (uint32_t q = 0; q < n0; ++q)
             issue(q);
@@ -231,6 +268,12 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
         const int wbase = wr * Cf::BW + offw + 32 * jb;                 // W at (j = jw, l = -d/2)
         const int vbase = Cf::VOFF / 8 + vrow * Cf::BV + offv;         // V at l = -d/2
         const int abase = ti.row0 ? wbase + DE / 2 : Cf::AOFF / 8 + 32 * jb; // A at j = jw
+        const int D = EXACT ? DE : p.D;
+        const int hd = D / 2; // a depth below DE computes the template's extra rows and columns, stores none
+        // A warp whose row has u + v outside the spectrum (every F(u+v) zero),
+        // or whose row or j block lies outside the stack's layout, only keeps
+        // the ring moving: its sums would be zero or unused.
+        const bool live = a0 < p.hw && jw < half_h && a0 + a2 < p.hw && (EXACT || a2 <= hd);
 
         float2 acc[8][Cf::TLW];
 #pragma unroll
@@ -250,30 +293,32 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
                 ok = false;
                 break;
             }
-            const float2* st = reinterpret_cast<const float2*>(smem + s * Cf::STAGE);
-            const float2* Wb = st + wbase + 8 * Cf::TLW * lb;
-            const float2* Vb = st + vbase + 8 * Cf::TLW * lb;
-            const float2* Ab = st + abase;
+            if (live) {
+                const float2* st = reinterpret_cast<const float2*>(smem + s * Cf::STAGE);
+                const float2* Wb = st + wbase + 8 * Cf::TLW * lb;
+                const float2* Vb = st + vbase + 8 * Cf::TLW * lb;
+                const float2* Ab = st + abase;
 
-            float2 A[8], V[Cf::TLW];
+                float2 A[8], V[Cf::TLW];
 #pragma unroll
-            for (int a = 0; a < 8; ++a)
-                A[a] = Ab[jg + 4 * a];
+                for (int a = 0; a < 8; ++a)
+                    A[a] = Ab[jg + 4 * a];
 #pragma unroll
-            for (int b = 0; b < Cf::TLW; ++b)
-                V[b] = b < nb ? Vb[lg + 8 * b] : make_float2(0.f, 0.f);
+                for (int b = 0; b < Cf::TLW; ++b)
+                    V[b] = b < nb ? Vb[lg + 8 * b] : make_float2(0.f, 0.f);
 #pragma unroll
-            for (int m = 0; m < Cf::NWV; ++m) {
-                const float2 w = Wb[jg + lg + 4 * m];
+                for (int m = 0; m < Cf::NWV; ++m) {
+                    const float2 w = Wb[jg + lg + 4 * m];
 #pragma unroll
-                for (int b = 0; b < Cf::TLW; ++b) {
-                    const int a = m - 2 * b;
-                    if (a >= 0 && a < 8 && b < nb)
-                        cmac(acc[a][b], A[a], V[b], w);
+                    for (int b = 0; b < Cf::TLW; ++b) {
+                        const int a = m - 2 * b;
+                        if (a >= 0 && a < 8 && b < nb)
+                            cmac(acc[a][b], A[a], V[b], w);
+                    }
                 }
+                if (edge) // l = +d/2 column, j = jw + lane
+                    cmac(acce, st[abase + lane], st[vbase + DE], st[wbase + DE + lane]);
             }
-            if (edge) // l = +d/2 column, j = jw + lane
-                cmac(acce, st[abase + lane], st[vbase + DE], st[wbase + DE + lane]);
             // Each thread releases the stage itself: its arrive (release
             // semantics) orders its own shared-memory reads before the refill.
             // A single arrive per warp after __syncwarp measured unsafe: the
@@ -347,9 +392,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
             if (threadIdx.x == 0)
                 p.tile_cnt[s_tile - p.nfull] = 0; // ready for the next launch
         }
-        const int D = EXACT ? DE : p.D;
-        const int hd = D / 2; // a depth below DE computes the template's extra rows and columns, stores none
-        if (a0 < p.hw && jw < half_h && (EXACT || a2 <= hd)) {
+        if (live) {
             // Kahan-compensated add of the batch partial into (B, C); within a
             // j step every load is issued before the first store (B and C never
             // alias).
@@ -479,7 +522,11 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
     a.D = g.De;
     a.nchm = (g.De / 2 + Cf::RPC - 1) / Cf::RPC;
     a.njt = (g.H + Cf::JT - 1) / Cf::JT;
-    a.nmain = g.hw * a.njt * a.nchm;
+    a.areg = std::max(0, g.hw - 1 - (a.nchm - 1) * Cf::RPC);
+    a.nreg = a.areg * a.njt * a.nchm;
+    a.nmain = a.nreg;
+    for (int a0 = a.areg; a0 < g.hw; ++a0)
+        a.nmain += main_chunks<DE>(a0, g.hw, a.nchm) * a.njt;
     a.ntiles = a.nmain + (g.hw + Cf::RPC - 1) / Cf::RPC * a.njt;
     // One CTA per unit (not persistent, so the block scheduler can place tiles
     // on whichever SMs are free, also while other streams' kernels run).  The
