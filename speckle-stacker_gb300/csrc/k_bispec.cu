@@ -70,15 +70,16 @@ struct BCfg {
     static constexpr int NWV = 8 + 2 * (TLW - 1);          // W values per thread per frame
     static constexpr int BW = JT + DE + 2;                 // W box columns (even start)
     static constexpr int BV = DE + 2;                      // V box columns (even start)
-    static constexpr int WBYTES = RPC * BW * 8;
+    static constexpr int FPS = 2;                          // frames per ring stage
+    static constexpr int WBYTES = RPC * BW * 8;            // one frame's boxes
     static constexpr int VBYTES = RPC * BV * 8;
     static constexpr int ABYTES = JT * 8;
     static constexpr int WOFF = 0;
-    static constexpr int VOFF = (WBYTES + 127) / 128 * 128;
-    static constexpr int AOFF = VOFF + (VBYTES + 127) / 128 * 128;
-    static constexpr int STAGE = AOFF + (ABYTES + 127) / 128 * 128;
+    static constexpr int VOFF = (FPS * WBYTES + 127) / 128 * 128;
+    static constexpr int AOFF = VOFF + (FPS * VBYTES + 127) / 128 * 128;
+    static constexpr int STAGE = AOFF + (FPS * ABYTES + 127) / 128 * 128;
     static constexpr int NSR = (200 * 1024) / STAGE;       // ~200 KB of frame stages
-    static constexpr int NS = NSR > 16 ? 16 : (NSR < 4 ? 4 : NSR);
+    static constexpr int NS = NSR >= 16 ? 16 : (NSR >= 8 ? 8 : 4); // a power of two
     static constexpr int SMEM = NS * STAGE + 2 * NS * 8 + 16;
     static_assert(RPC * NLB * NJB == WARPS && ROWS % RPC == 0, "task split");
     static_assert(BW <= 256 && NS > kLag + 1, "box / ring");
@@ -201,25 +202,27 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
     auto split_f0 = [&]() { return (int)((long long)(split_s() % p.P) * nf / p.P); };
     auto split_f1 = [&]() { return (int)((long long)(split_s() % p.P + 1) * nf / p.P); };
     const uint32_t total = split_unit ? (uint32_t)(split_f1() - split_f0()) : (uint32_t)nf;
+    const uint32_t niter = (total + Cf::FPS - 1) / Cf::FPS; // ring iterations (FPS frames each)
     const int cv = (half_h - DE / 2) & ~1;
     const int offv = (half_h - DE / 2) - cv;
 
     // box coordinates of this CTA's tile, set once by thread 0 (x in 8-byte
-    // elements, even: 16-byte aligned); iteration r loads frame f0 + r
+    // elements, even: 16-byte aligned); iteration r loads frames f0 + FPS r ..
+    // f0 + FPS r + FPS - 1 (one box per operand, frames outermost)
     __shared__ int s_box[7]; // W x, W y, V y, A x, A y, f0, row-0 tile
 
     // issue the loads of iteration r into stage r % NS
     auto issue = [&](uint32_t r) {
-        const int f = s_box[5] + (int)r;
+        const int f = s_box[5] + Cf::FPS * (int)r;
         const int s = r % Cf::NS;
         unsigned char* st = smem + s * Cf::STAGE;
         if (!s_box[6]) {
-            mbar_arrive_expect_tx(&full[s], Cf::WBYTES + Cf::VBYTES + Cf::ABYTES);
+            mbar_arrive_expect_tx(&full[s], Cf::FPS * (Cf::WBYTES + Cf::VBYTES + Cf::ABYTES));
             tma_load_3d(st + Cf::WOFF, &tmW, s_box[0], s_box[1], f, &full[s]);
             tma_load_3d(st + Cf::VOFF, &tmV, cv, s_box[2], f, &full[s]);
             tma_load_3d(st + Cf::AOFF, &tmA, s_box[3], s_box[4], f, &full[s]);
         } else {
-            mbar_arrive_expect_tx(&full[s], Cf::WBYTES + Cf::VBYTES);
+            mbar_arrive_expect_tx(&full[s], Cf::FPS * (Cf::WBYTES + Cf::VBYTES));
             tma_load_3d(st + Cf::WOFF, &tmW, s_box[0], s_box[1], f, &full[s]);
             tma_load_3d(st + Cf::VOFF, &tmV, cv, s_box[2], f, &full[s]);
         }
@@ -237,7 +240,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
         s_box[4] = ti.a0;
         s_box[5] = split_unit ? split_f0() : 0;
         s_box[6] = ti.row0;
-        const uint32_t n0 = total < kAhead ? total : kAhead;
+        const uint32_t n0 = niter < kAhead ? niter : kAhead;
         for (uint32_t q = 0; q < n0; ++q)
             issue(q);
         *hi_issued = n0;
@@ -283,7 +286,35 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
                 acc[a][b] = make_float2(0.f, 0.f);
         float2 acce = make_float2(0.f, 0.f);
 
-        for (int f = 0; f < nfu; ++f, ++r) {
+        // one frame of the stage: boxes at W, V, A (the row-0 tiles' A is in the W box)
+        auto frame = [&](const float2* Wf, const float2* Vf, const float2* Af) {
+            const float2* Wb = Wf + wbase + 8 * Cf::TLW * lb;
+            const float2* Vb = Vf + vbase + 8 * Cf::TLW * lb;
+            const float2* Ab = Af + abase;
+            float2 A[8], V[Cf::TLW];
+#pragma unroll
+            for (int a = 0; a < 8; ++a)
+                A[a] = Ab[jg + 4 * a];
+#pragma unroll
+            for (int b = 0; b < Cf::TLW; ++b)
+                V[b] = b < nb ? Vb[lg + 8 * b] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int m = 0; m < Cf::NWV; ++m) {
+                const float2 w = Wb[jg + lg + 4 * m];
+#pragma unroll
+                for (int b = 0; b < Cf::TLW; ++b) {
+                    const int a = m - 2 * b;
+                    if (a >= 0 && a < 8 && b < nb)
+                        cmac(acc[a][b], A[a], V[b], w);
+                }
+            }
+            if (edge) // l = +d/2 column, j = jw + lane
+                cmac(acce, Af[abase + lane], Vf[vbase + DE], Wf[wbase + DE + lane]);
+        };
+        // the second frame's A box: in the W box for row-0 tiles
+        const int astep = ti.row0 ? Cf::WBYTES / 8 : Cf::ABYTES / 8;
+
+        for (uint32_t q = 0; q < niter; ++q, ++r) {
             const int s = r % Cf::NS;
             // every lane waits; the warp leaves together if any lane timed out
             const bool got = mbar_wait_bounded(&full[s], (r / Cf::NS) & 1, kWaitNs);
@@ -295,29 +326,9 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
             }
             if (live) {
                 const float2* st = reinterpret_cast<const float2*>(smem + s * Cf::STAGE);
-                const float2* Wb = st + wbase + 8 * Cf::TLW * lb;
-                const float2* Vb = st + vbase + 8 * Cf::TLW * lb;
-                const float2* Ab = st + abase;
-
-                float2 A[8], V[Cf::TLW];
-#pragma unroll
-                for (int a = 0; a < 8; ++a)
-                    A[a] = Ab[jg + 4 * a];
-#pragma unroll
-                for (int b = 0; b < Cf::TLW; ++b)
-                    V[b] = b < nb ? Vb[lg + 8 * b] : make_float2(0.f, 0.f);
-#pragma unroll
-                for (int m = 0; m < Cf::NWV; ++m) {
-                    const float2 w = Wb[jg + lg + 4 * m];
-#pragma unroll
-                    for (int b = 0; b < Cf::TLW; ++b) {
-                        const int a = m - 2 * b;
-                        if (a >= 0 && a < 8 && b < nb)
-                            cmac(acc[a][b], A[a], V[b], w);
-                    }
-                }
-                if (edge) // l = +d/2 column, j = jw + lane
-                    cmac(acce, st[abase + lane], st[vbase + DE], st[wbase + DE + lane]);
+                frame(st, st, st);
+                if (Cf::FPS * q + 1 < (uint32_t)nfu) // a unit's odd last frame: the box's second frame is not its own
+                    frame(st + Cf::WBYTES / 8, st + Cf::VBYTES / 8, st + astep);
             }
             // Each thread releases the stage itself: its arrive (release
             // semantics) orders its own shared-memory reads before the refill.
@@ -326,7 +337,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
             mbar_arrive(&empty[s]);
             __syncwarp();
             if (r + kAhead == nr) { // ring refill, round robin over the warps
-                if (!stop && nr < total) {
+                if (!stop && nr < niter) {
                     bool go = true;
                     if (lane == 0) {
                         const uint32_t prev = r - kLag; // the iteration that last used the stage
@@ -484,15 +495,15 @@ static EncodeTiledFn get_encode()
 }
 
 // S viewed as UINT64 (one complex<float> per element) [nframes][hw][H];
-// box = {bcols, brows, 1 frame}.
-static bool make_map(CUtensorMap* m, const float2* S, int nframes, const Geometry& g, int bcols, int brows)
+// box = {bcols, brows, nfb frames}.
+static bool make_map(CUtensorMap* m, const float2* S, int nframes, const Geometry& g, int bcols, int brows, int nfb)
 {
     EncodeTiledFn enc = get_encode();
     if (!enc)
         return false;
     const cuuint64_t dims[3] = { (cuuint64_t)g.H, (cuuint64_t)g.hw, (cuuint64_t)nframes };
     const cuuint64_t strides[2] = { (cuuint64_t)g.H * 8, (cuuint64_t)g.H * 8 * g.hw };
-    const cuuint32_t box[3] = { (cuuint32_t)bcols, (cuuint32_t)brows, 1 };
+    const cuuint32_t box[3] = { (cuuint32_t)bcols, (cuuint32_t)brows, (cuuint32_t)nfb };
     const cuuint32_t es[3] = { 1, 1, 1 };
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<float2*>(S), dims, strides, box, es,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -505,8 +516,9 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
 {
     using Cf = BCfg<DE>;
     CUtensorMap mW, mV, mA;
-    if (!make_map(&mW, L.S, L.nframes, g, Cf::BW, Cf::RPC) || !make_map(&mV, L.S, L.nframes, g, Cf::BV, Cf::RPC)
-        || !make_map(&mA, L.S, L.nframes, g, Cf::JT, 1))
+    if (!make_map(&mW, L.S, L.nframes, g, Cf::BW, Cf::RPC, Cf::FPS)
+        || !make_map(&mV, L.S, L.nframes, g, Cf::BV, Cf::RPC, Cf::FPS)
+        || !make_map(&mA, L.S, L.nframes, g, Cf::JT, 1, Cf::FPS))
         return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(bispec_accum_kernel<DE, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          Cf::SMEM);
