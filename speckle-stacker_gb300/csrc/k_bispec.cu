@@ -70,7 +70,7 @@ struct BCfg {
     static constexpr int NWV = 8 + 2 * (TLW - 1);          // W values per thread per frame
     static constexpr int BW = JT + DE + 2;                 // W box columns (even start)
     static constexpr int BV = DE + 2;                      // V box columns (even start)
-    static constexpr int FPS = 2;                          // frames per ring stage
+    static constexpr int FPS = 4;                          // frames per ring stage
     static constexpr int WBYTES = RPC * BW * 8;            // one frame's boxes
     static constexpr int VBYTES = RPC * BV * 8;
     static constexpr int ABYTES = JT * 8;
@@ -79,10 +79,10 @@ struct BCfg {
     static constexpr int AOFF = VOFF + (FPS * VBYTES + 127) / 128 * 128;
     static constexpr int STAGE = AOFF + (FPS * ABYTES + 127) / 128 * 128;
     static constexpr int NSR = (200 * 1024) / STAGE;       // ~200 KB of frame stages
-    static constexpr int NS = NSR >= 16 ? 16 : (NSR >= 8 ? 8 : 4); // a power of two
+    static constexpr int NS = NSR > 16 ? 16 : (NSR < 4 ? 4 : NSR);
     static constexpr int SMEM = NS * STAGE + 2 * NS * 8 + 16;
     static_assert(RPC * NLB * NJB == WARPS && ROWS % RPC == 0, "task split");
-    static_assert(BW <= 256 && NS > kLag + 1, "box / ring");
+    static_assert(BW <= 256 && NS > kLag + 1 && SMEM <= 227 * 1024, "box / ring");
 };
 
 struct BispecArgs {
@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
             if (edge) // l = +d/2 column, j = jw + lane
                 cmac(acce, Af[abase + lane], Vf[vbase + DE], Wf[wbase + DE + lane]);
         };
-        // the second frame's A box: in the W box for row-0 tiles
+        // the A box step between frames: in the W box for row-0 tiles
         const int astep = ti.row0 ? Cf::WBYTES / 8 : Cf::ABYTES / 8;
 
         for (uint32_t q = 0; q < niter; ++q, ++r) {
@@ -327,8 +327,10 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
             if (live) {
                 const float2* st = reinterpret_cast<const float2*>(smem + s * Cf::STAGE);
                 frame(st, st, st);
-                if (Cf::FPS * q + 1 < (uint32_t)nfu) // a unit's odd last frame: the box's second frame is not its own
-                    frame(st + Cf::WBYTES / 8, st + Cf::VBYTES / 8, st + astep);
+#pragma unroll
+                for (int k = 1; k < Cf::FPS; ++k) // a unit's last stage may hold frames that are not its own
+                    if (Cf::FPS * q + k < (uint32_t)nfu)
+                        frame(st + k * (Cf::WBYTES / 8), st + k * (Cf::VBYTES / 8), st + k * astep);
             }
             // Each thread releases the stage itself: its arrive (release
             // semantics) orders its own shared-memory reads before the refill.
