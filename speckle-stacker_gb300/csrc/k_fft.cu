@@ -60,9 +60,8 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const T* __restrict__ fra
     const int y0 = blockIdx.x * kRowBlock;
     const T* fr = frames + (long long)f * fstride + (long long)y0 * W;
     load_twiddles(tw, tw_g, kTwLog);
-    for (int idx = threadIdx.x; idx < kRowBlock * W; idx += blockDim.x) {
+    auto put = [&](int idx, float2 v) {
         const int r = idx >> logW, x = idx & (W - 1);
-        const float2 v = pix_df(fr, idx);
         dfc& d = lines[(r >> 1) * LW + pad8(bitrev(x, logW))];
         if (r & 1) {
             d.h.y = v.x;
@@ -71,6 +70,21 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const T* __restrict__ fra
             d.h.x = v.x;
             d.l.x = v.y;
         }
+    };
+    // 16-byte loads (16, 8 or 4 pixels) when the rows allow; W >= 16 keeps a
+    // vector inside one row
+    constexpr int PV = sizeof(T) <= 4 ? 16 / (int)sizeof(T) : 1;
+    if (PV > 1 && (reinterpret_cast<uintptr_t>(fr) & 15) == 0) {
+        for (int i0 = threadIdx.x * PV; i0 < kRowBlock * W; i0 += blockDim.x * PV) {
+            T px[PV];
+            *reinterpret_cast<uint4*>(px) = *reinterpret_cast<const uint4*>(fr + i0);
+#pragma unroll
+            for (int e = 0; e < PV; ++e)
+                put(i0 + e, make_float2((float)px[e], 0.f));
+        }
+    } else {
+        for (int idx = threadIdx.x; idx < kRowBlock * W; idx += blockDim.x)
+            put(idx, pix_df(fr, idx));
     }
     __syncthreads();
     fft_passes(lines, logW, kRowBlock / 2, LW, tw, kTwLog, -1);
@@ -81,11 +95,11 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const T* __restrict__ fra
         const dfc za = Z[pad8(a)], zb = Z[pad8((W - a) & (W - 1))];
         dfc g;
         if ((r & 1) == 0) { // conj of X0 = (Z(a) + conj Z(-a)) / 2
-            df_add(za.h.x, za.l.x, zb.h.x, zb.l.x, g.h.x, g.l.x);
-            df_add(zb.h.y, zb.l.y, -za.h.y, -za.l.y, g.h.y, g.l.y);
+            df_add_lazy(za.h.x, za.l.x, zb.h.x, zb.l.x, g.h.x, g.l.x);
+            df_add_lazy(zb.h.y, zb.l.y, -za.h.y, -za.l.y, g.h.y, g.l.y);
         } else { // conj of X1 = (Z(a) - conj Z(-a)) / 2i
-            df_add(za.h.y, za.l.y, zb.h.y, zb.l.y, g.h.x, g.l.x);
-            df_add(za.h.x, za.l.x, -zb.h.x, -zb.l.x, g.h.y, g.l.y);
+            df_add_lazy(za.h.y, za.l.y, zb.h.y, zb.l.y, g.h.x, g.l.x);
+            df_add_lazy(za.h.x, za.l.x, -zb.h.x, -zb.l.x, g.h.y, g.l.y);
         }
         g.h.x *= 0.5f; g.l.x *= 0.5f; g.h.y *= 0.5f; g.l.y *= 0.5f;
         out[(long long)a * H + y0 + r] = g;
@@ -148,7 +162,9 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __re
         for (int c = threadIdx.x; c < H; c += blockDim.x) {
             float ah = pacc[c].x, al = pacc[c].y;
             for (int l = 0; l < nl; ++l) {
-                const dfc v = L1[l * LH + pad8((c + H / 2) & (H - 1))];
+                dfc v = L1[l * LH + pad8((c + H / 2) & (H - 1))];
+                df_norm(v.h.x, v.l.x); // the FFT leaves lazy pairs
+                df_norm(v.h.y, v.l.y);
                 float rh, rl, ih, il, sh, sl;
                 df_mul(v.h.x, v.l.x, v.h.x, v.l.x, rh, rl);
                 df_mul(v.h.y, v.l.y, v.h.y, v.l.y, ih, il);

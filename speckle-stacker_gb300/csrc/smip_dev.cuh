@@ -93,32 +93,70 @@ __device__ __forceinline__ void df_mul(float ah, float al, float bh, float bl, f
     rl = __fsub_rn(e, __fsub_rn(rh, p));
 }
 
+// The FFT butterflies below keep their values as unevaluated pairs hi + lo
+// and skip the renormalisation (hi, lo) -> (fl(hi + lo), rest) after each
+// operation: every hi + hi is still an error-free two_sum and every product
+// an FMA-exact two_prod, and the lo words (a few ulps of hi) only collect
+// those errors and the cross terms, so the pair keeps ~44-bit accuracy at
+// 64 instead of 94 FP32 operations per butterfly.  Consumers round hi + lo
+// once (df_round) or renormalise with df_norm before a product of pairs.
+__device__ __forceinline__ void df_norm(float& h, float& l)
+{
+    float s, e;
+    two_sum(h, l, s, e);
+    h = s;
+    l = e;
+}
+
+__device__ __forceinline__ void df_add_lazy(float ah, float al, float bh, float bl, float& rh, float& rl)
+{
+    float s, e;
+    two_sum(ah, bh, s, e);
+    rh = s;
+    rl = __fadd_rn(e, __fadd_rn(al, bl));
+}
+
 __device__ __forceinline__ dfc df_cadd(const dfc& a, const dfc& b)
 {
     dfc r;
-    df_add(a.h.x, a.l.x, b.h.x, b.l.x, r.h.x, r.l.x);
-    df_add(a.h.y, a.l.y, b.h.y, b.l.y, r.h.y, r.l.y);
+    df_add_lazy(a.h.x, a.l.x, b.h.x, b.l.x, r.h.x, r.l.x);
+    df_add_lazy(a.h.y, a.l.y, b.h.y, b.l.y, r.h.y, r.l.y);
     return r;
 }
 
 __device__ __forceinline__ dfc df_csub(const dfc& a, const dfc& b)
 {
     dfc r;
-    df_add(a.h.x, a.l.x, -b.h.x, -b.l.x, r.h.x, r.l.x);
-    df_add(a.h.y, a.l.y, -b.h.y, -b.l.y, r.h.y, r.l.y);
+    df_add_lazy(a.h.x, a.l.x, -b.h.x, -b.l.x, r.h.x, r.l.x);
+    df_add_lazy(a.h.y, a.l.y, -b.h.y, -b.l.y, r.h.y, r.l.y);
     return r;
+}
+
+// (a1 b1 - a2 b2) as a lazy pair: both products exact as (p, FMA residual),
+// the cross terms with the lo words folded into the residual sum, and the
+// difference of the two high products an error-free two_sum.  The lo * lo
+// terms are dropped (below 2^-48 of the products; twiddles are normalised).
+__device__ __forceinline__ void df_dot2_lazy(float a1h, float a1l, float b1h, float b1l, float a2h, float a2l,
+                                             float b2h, float b2l, float& rh, float& rl)
+{
+    const float p1 = __fmul_rn(a1h, b1h);
+    const float p2 = __fmul_rn(a2h, b2h);
+    float t = __fsub_rn(fmaf(a1h, b1h, -p1), fmaf(a2h, b2h, -p2));
+    t = fmaf(a1h, b1l, t);
+    t = fmaf(a1l, b1h, t);
+    t = fmaf(-a2h, b2l, t);
+    t = fmaf(-a2l, b2h, t);
+    float s, e;
+    two_sum(p1, -p2, s, e);
+    rh = s;
+    rl = __fadd_rn(t, e);
 }
 
 __device__ __forceinline__ dfc df_cmul(const dfc& a, const dfc& w)
 {
-    float p1h, p1l, p2h, p2l, p3h, p3l, p4h, p4l;
-    df_mul(a.h.x, a.l.x, w.h.x, w.l.x, p1h, p1l);
-    df_mul(a.h.y, a.l.y, w.h.y, w.l.y, p2h, p2l);
-    df_mul(a.h.x, a.l.x, w.h.y, w.l.y, p3h, p3l);
-    df_mul(a.h.y, a.l.y, w.h.x, w.l.x, p4h, p4l);
     dfc r;
-    df_add(p1h, p1l, -p2h, -p2l, r.h.x, r.l.x);
-    df_add(p3h, p3l, p4h, p4l, r.h.y, r.l.y);
+    df_dot2_lazy(a.h.x, a.l.x, w.h.x, w.l.x, a.h.y, a.l.y, w.h.y, w.l.y, r.h.x, r.l.x);   // re
+    df_dot2_lazy(a.h.x, a.l.x, w.h.y, w.l.y, -a.h.y, -a.l.y, w.h.x, w.l.x, r.h.y, r.l.y); // im
     return r;
 }
 
