@@ -48,14 +48,16 @@ __device__ __forceinline__ float2 df_round(const dfc& v) { return make_float2(v.
 // half-spectra are separated afterwards.  Output G'(a, y) = sum_x f(x, y)
 // exp(+2 pi i a x / W), float-float, stored [f][a][y].
 template <typename T>
-__global__ void __launch_bounds__(256) row_pass_kernel(const T* __restrict__ frames, long long fstride, int logW, int H,
+__global__ void __launch_bounds__(256, 4) row_pass_kernel(const T* __restrict__ frames, long long fstride, int logW, int H,
                                                         int hw, dfc* __restrict__ Gt, const dfc* __restrict__ tw_g)
 {
     extern __shared__ dfc smdf[];
     dfc* tw = smdf;                                // 2^(kTwLog-1)
     dfc* lines = smdf + (1 << (kTwLog - 1));       // [kRowBlock/2][pad8(W)]
     const int W = 1 << logW;
-    const int LW = pad8(W);
+    // one spare element per line: the output pass reads the same element of
+    // the 8 lines in one warp, which a 128-byte multiple would put in one bank
+    const int LW = pad8(W) + 1;
     const int f = blockIdx.y;
     const int y0 = blockIdx.x * kRowBlock;
     const T* fr = frames + (long long)f * fstride + (long long)y0 * W;
@@ -71,16 +73,26 @@ __global__ void __launch_bounds__(256) row_pass_kernel(const T* __restrict__ fra
             d.l.x = v.y;
         }
     };
-    // 16-byte loads (16, 8 or 4 pixels) when the rows allow; W >= 16 keeps a
-    // vector inside one row
+    // 16-byte loads (16, 8 or 4 pixels; W >= 16 keeps a vector inside one
+    // row) of both rows of a line, stored as whole complex values: a warp's
+    // stores of one vector element go to 32 bit-reversed slots that the
+    // padding spreads over all banks
     constexpr int PV = sizeof(T) <= 4 ? 16 / (int)sizeof(T) : 1;
     if (PV > 1 && (reinterpret_cast<uintptr_t>(fr) & 15) == 0) {
-        for (int i0 = threadIdx.x * PV; i0 < kRowBlock * W; i0 += blockDim.x * PV) {
-            T px[PV];
-            *reinterpret_cast<uint4*>(px) = *reinterpret_cast<const uint4*>(fr + i0);
+        const int vpl = W / PV; // vectors per row
+        for (int i = threadIdx.x; i < (kRowBlock / 2) * vpl; i += blockDim.x) {
+            const int pr = i / vpl, x0 = (i - pr * vpl) * PV;
+            T p0[PV], p1[PV];
+            *reinterpret_cast<uint4*>(p0) = *reinterpret_cast<const uint4*>(fr + (2 * pr) * W + x0);
+            *reinterpret_cast<uint4*>(p1) = *reinterpret_cast<const uint4*>(fr + (2 * pr + 1) * W + x0);
+            dfc* L = lines + pr * LW;
 #pragma unroll
-            for (int e = 0; e < PV; ++e)
-                put(i0 + e, make_float2((float)px[e], 0.f));
+            for (int e = 0; e < PV; ++e) {
+                dfc d;
+                d.h = make_float2((float)p0[e], (float)p1[e]);
+                d.l = make_float2(0.f, 0.f);
+                L[pad8(bitrev(x0 + e, logW))] = d;
+            }
         }
     } else {
         for (int idx = threadIdx.x; idx < kRowBlock * W; idx += blockDim.x)
@@ -141,9 +153,15 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __re
     for (int f0 = fbeg; f0 < fend; f0 += kColLines) {
         const int nl = min(kColLines, fend - f0);
         __syncthreads();
-        for (int idx = threadIdx.x; idx < nl * H; idx += blockDim.x) {
-            const int l = idx >> logH, y = idx & (H - 1);
-            L1[l * LH + pad8(bitrev(y, logH))] = Gt[(f0 + l) * gstride + (long long)a * H + y];
+        // eight consecutive y per thread: a warp's stores of one of them go to
+        // 32 bit-reversed slots that the padding spreads over all banks
+        for (int i = threadIdx.x; i < nl * (H / 8); i += blockDim.x) {
+            const int l = i / (H / 8), y0 = (i - l * (H / 8)) * 8;
+            const dfc* src = Gt + (f0 + l) * gstride + (long long)a * H + y0;
+            dfc* L = L1 + l * LH;
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+                L[pad8(bitrev(y0 + e, logH))] = src[e];
         }
         __syncthreads();
         fft_passes(L1, logH, nl, LH, twd, kTwLog, -1);
@@ -213,9 +231,13 @@ __global__ void __launch_bounds__(256) xcorr_rows_kernel(const float2* __restric
 {
     extern __shared__ float2 sm[];
     const int W = 1 << logW;
+    // Ts rows padded to kRowBlock + 1: the Hermitian build below reads one
+    // column r of consecutive a per warp, which an unpadded 128-byte row
+    // stride would put in one bank pair
+    constexpr int TS = kRowBlock + 1;
     float2* tw = sm;
-    float2* Ts = tw + (1 << (kTwLog - 1));         // [hw][kRowBlock]
-    float2* lines = Ts + hw * kRowBlock;           // [kRowBlock/2][pad8(W)]
+    float2* Ts = tw + (1 << (kTwLog - 1));         // [hw][TS]
+    float2* lines = Ts + hw * TS;                  // [kRowBlock/2][pad8(W)]
     const int LW = pad8(W);
     const int f = blockIdx.y;
     const int y0 = blockIdx.x * kRowBlock;
@@ -223,7 +245,7 @@ __global__ void __launch_bounds__(256) xcorr_rows_kernel(const float2* __restric
     load_twiddles(tw, tw_g, kTwLog);
     for (int idx = threadIdx.x; idx < hw * kRowBlock; idx += blockDim.x) {
         const int a = idx / kRowBlock, r = idx - a * kRowBlock;
-        Ts[idx] = T[(long long)a * H + y0 + r];
+        Ts[a * TS + r] = T[(long long)a * H + y0 + r];
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < (kRowBlock / 2) * W; idx += blockDim.x) {
@@ -233,13 +255,13 @@ __global__ void __launch_bounds__(256) xcorr_rows_kernel(const float2* __restric
         for (int h = 0; h < 2; ++h) {
             const int r = 2 * p + h;
             if (k == 0)
-                z[h] = make_float2(Ts[0 * kRowBlock + r].x, 0.f);
+                z[h] = make_float2(Ts[r].x, 0.f);
             else if (k < W / 2)
-                z[h] = cconj(Ts[k * kRowBlock + r]);
+                z[h] = cconj(Ts[k * TS + r]);
             else if (k == W / 2)
-                z[h] = make_float2(Ts[(W / 2) * kRowBlock + r].x, 0.f);
+                z[h] = make_float2(Ts[(W / 2) * TS + r].x, 0.f);
             else
-                z[h] = Ts[(W - k) * kRowBlock + r];
+                z[h] = Ts[(W - k) * TS + r];
         }
         lines[p * LW + pad8(bitrev(k, logW))] = make_float2(z[0].x - z[1].y, z[0].y + z[1].x);
     }
@@ -289,7 +311,7 @@ cudaError_t launch_row_pass(int dtype, const void* frames, long long fstride, in
                             const dfc* twdf, cudaStream_t st)
 {
     const dim3 grid(g.H / kRowBlock, nframes);
-    const size_t smem = sizeof(dfc) * ((1 << (kTwLog - 1)) + (kRowBlock / 2) * pad8(g.W));
+    const size_t smem = sizeof(dfc) * ((1 << (kTwLog - 1)) + (kRowBlock / 2) * (pad8(g.W) + 1));
     cudaError_t e = cudaSuccess;
     switch (dtype) {
     case 0:
@@ -342,7 +364,7 @@ cudaError_t launch_xcorr_rows(const float2* T, float* corr, int nframes, const G
                               cudaStream_t st)
 {
     const dim3 grid(g.H / kRowBlock, nframes);
-    const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + g.hw * kRowBlock + (kRowBlock / 2) * pad8(g.W));
+    const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + g.hw * (kRowBlock + 1) + (kRowBlock / 2) * pad8(g.W));
     cudaError_t e = allow_smem(xcorr_rows_kernel, smem);
     if (e != cudaSuccess)
         return e;

@@ -298,6 +298,22 @@ def test_load_bispectrum_resume(smip, tmp_path):
         e.load_bispectrum(str(tmp_path / "missing.dat"))
 
 
+def test_weak_bins_keep_fp32_accuracy(smip):
+    """The forward FFT is float-float: every power-spectrum bin down to 1e-8 of
+    the strongest keeps 1e-6 relative accuracy against an FP64 FFT of the same
+    256x256 u16 speckle frame (a plain FP32 FFT is off by ~1e-2 there)."""
+    from smip_gb300 import synthetic as S
+
+    fr = S.make_stack(S.config_spec("extended256", nframes=1), 0, 1)
+    with smip.Stack(256, 256, 32) as st:
+        st.push_frames(fr)
+        P = st.power()
+    F2 = np.abs(np.fft.fft2(fr[0].astype(np.float64))) ** 2 / fr[0].size
+    m = F2 >= 1e-8 * F2.max()
+    rel = np.abs(P[m] - F2[m]) / F2[m]
+    assert rel.max() <= 1e-6, rel.max()
+
+
 def test_full_size_properties(smip):
     """256x256 u16, depth 32, 64 frames: size-independent checks against
     float64 numpy on the same frames (no oracle at this size)."""
