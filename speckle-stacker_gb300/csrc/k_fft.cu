@@ -52,16 +52,16 @@ __global__ void __launch_bounds__(256, 4) row_pass_kernel(const T* __restrict__ 
                                                         int hw, dfc* __restrict__ Gt, const dfc* __restrict__ tw_g)
 {
     extern __shared__ dfc smdf[];
-    dfc* tw = smdf;                                // 2^(kTwLog-1)
-    dfc* lines = smdf + (1 << (kTwLog - 1));       // [kRowBlock/2][pad8(W)]
     const int W = 1 << logW;
+    dfc* tw = smdf;                                // W - 1, stage-packed (+1 spare)
+    dfc* lines = smdf + W;                         // [kRowBlock/2][pad8(W) + 1]
     // one spare element per line: the output pass reads the same element of
     // the 8 lines in one warp, which a 128-byte multiple would put in one bank
     const int LW = pad8(W) + 1;
     const int f = blockIdx.y;
     const int y0 = blockIdx.x * kRowBlock;
     const T* fr = frames + (long long)f * fstride + (long long)y0 * W;
-    load_twiddles(tw, tw_g, kTwLog);
+    load_twiddles_packed(tw, tw_g, logW, kTwLog);
     auto put = [&](int idx, float2 v) {
         const int r = idx >> logW, x = idx & (W - 1);
         dfc& d = lines[(r >> 1) * LW + pad8(bitrev(x, logW))];
@@ -131,11 +131,11 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __re
 {
     extern __shared__ dfc smdf[];
     const int H = 1 << logH;
-    dfc* twd = smdf;                                               // 2^(kTwLog-1)
+    dfc* twd = smdf;                                               // H - 1, stage-packed (+1 spare)
     const int LH = pad8(H);                                        // padded line length
-    dfc* L1 = twd + (1 << (kTwLog - 1));                           // [kColLines][LH]
-    float2* tw = reinterpret_cast<float2*>(L1 + kColLines * LH);   // 2^(kTwLog-1)
-    float2* R = tw + (1 << (kTwLog - 1));                          // [H]
+    dfc* L1 = twd + H;                                             // [kColLines][LH]
+    float2* tw = reinterpret_cast<float2*>(L1 + kColLines * LH);   // H - 1, stage-packed (+1 spare)
+    float2* R = tw + H;                                            // [H]
     float2* L2 = R + H;                                            // [kColLines][LH]
     float2* pacc = reinterpret_cast<float2*>(L2 + kColLines * LH); // [H] float-float (hi, lo)
     const int a = blockIdx.x;
@@ -143,8 +143,8 @@ __global__ void __launch_bounds__(256) col_pass_kernel(int mode, const dfc* __re
     const int fbeg = chunk * fpc;
     const int fend = min(nframes, fbeg + fpc);
     const long long gstride = (long long)hw * H;
-    load_twiddles(twd, twdf_g, kTwLog);
-    load_twiddles(tw, tw_g, kTwLog);
+    load_twiddles_packed(twd, twdf_g, logH, kTwLog);
+    load_twiddles_packed(tw, tw_g, logH, kTwLog);
     if (mode == 0)
         for (int y = threadIdx.x; y < H; y += blockDim.x) {
             R[y] = Rbuf[(long long)a * H + y];
@@ -235,14 +235,14 @@ __global__ void __launch_bounds__(256) xcorr_rows_kernel(const float2* __restric
     // column r of consecutive a per warp, which an unpadded 128-byte row
     // stride would put in one bank pair
     constexpr int TS = kRowBlock + 1;
-    float2* tw = sm;
-    float2* Ts = tw + (1 << (kTwLog - 1));         // [hw][TS]
+    float2* tw = sm;                               // W - 1, stage-packed (+1 spare)
+    float2* Ts = tw + W;                           // [hw][TS]
     float2* lines = Ts + hw * TS;                  // [kRowBlock/2][pad8(W)]
     const int LW = pad8(W);
     const int f = blockIdx.y;
     const int y0 = blockIdx.x * kRowBlock;
     const float2* T = Gt + (long long)f * hw * H;
-    load_twiddles(tw, tw_g, kTwLog);
+    load_twiddles_packed(tw, tw_g, logW, kTwLog);
     for (int idx = threadIdx.x; idx < hw * kRowBlock; idx += blockDim.x) {
         const int a = idx / kRowBlock, r = idx - a * kRowBlock;
         Ts[a * TS + r] = T[(long long)a * H + y0 + r];
@@ -311,7 +311,7 @@ cudaError_t launch_row_pass(int dtype, const void* frames, long long fstride, in
                             const dfc* twdf, cudaStream_t st)
 {
     const dim3 grid(g.H / kRowBlock, nframes);
-    const size_t smem = sizeof(dfc) * ((1 << (kTwLog - 1)) + (kRowBlock / 2) * (pad8(g.W) + 1));
+    const size_t smem = sizeof(dfc) * (g.W + (kRowBlock / 2) * (pad8(g.W) + 1));
     cudaError_t e = cudaSuccess;
     switch (dtype) {
     case 0:
@@ -341,8 +341,8 @@ cudaError_t launch_col_pass(int mode, const dfc* Gt, float2* S, const float2* Rb
 {
     const int nchunks = mode == 1 ? 1 : (nframes + fpc - 1) / fpc;
     const dim3 grid(g.hw, nchunks);
-    const size_t smem = sizeof(dfc) * ((1 << (kTwLog - 1)) + kColLines * pad8(g.H))
-                        + sizeof(float2) * ((1 << (kTwLog - 1)) + g.H + kColLines * pad8(g.H)) + sizeof(double) * g.H;
+    const size_t smem = sizeof(dfc) * (g.H + kColLines * pad8(g.H))
+                        + sizeof(float2) * (g.H + g.H + kColLines * pad8(g.H)) + sizeof(double) * g.H;
     cudaError_t e = allow_smem(col_pass_kernel, smem);
     if (e != cudaSuccess)
         return e;
@@ -364,7 +364,7 @@ cudaError_t launch_xcorr_rows(const float2* T, float* corr, int nframes, const G
                               cudaStream_t st)
 {
     const dim3 grid(g.H / kRowBlock, nframes);
-    const size_t smem = sizeof(float2) * ((1 << (kTwLog - 1)) + g.hw * (kRowBlock + 1) + (kRowBlock / 2) * pad8(g.W));
+    const size_t smem = sizeof(float2) * (g.W + g.hw * (kRowBlock + 1) + (kRowBlock / 2) * pad8(g.W));
     cudaError_t e = allow_smem(xcorr_rows_kernel, smem);
     if (e != cudaSuccess)
         return e;

@@ -276,7 +276,6 @@ __device__ __forceinline__ void fft_pass(C* buf, int logn, int nl, int ls, const
 #pragma unroll
         for (int t = 1; t <= K; ++t) {
             const int hm = 1 << (t - 1);
-            const int tsh = twlog - (s0 + t);
 #pragma unroll
             for (int m0 = 0; m0 < (1 << K); ++m0) {
                 if (m0 & hm)
@@ -287,7 +286,7 @@ __device__ __forceinline__ void fft_pass(C* buf, int logn, int nl, int ls, const
                 } else if (FIRST && 4 * k == (1 << t)) {
                     bfly_mi(v[m0], v[m0 + hm], sign);             // w = exp(-i pi/2)
                 } else {
-                    C w = tw[((k << s0) + j) << tsh];
+                    C w = tw[(1 << (s0 + t - 1)) - 1 + (k << s0) + j]; // stage-packed table
                     if (sign > 0)
                         w = tw_conj(w);
                     bfly(v[m0], v[m0 + hm], w);
@@ -302,7 +301,8 @@ __device__ __forceinline__ void fft_pass(C* buf, int logn, int nl, int ls, const
 }
 
 // In-place DIT FFT of nl padded lines of length n = 2^logn (logn >= 3), input in
-// bit-reversed order, in passes of at most 3 stages.  Called by all threads.
+// bit-reversed order, in passes of at most 3 stages, twiddles from a
+// stage-packed table (load_twiddles_packed).  Called by all threads.
 template <typename C>
 __device__ void fft_passes(C* buf, int logn, int nl, int ls, const C* tw, int twlog, int sign)
 {
@@ -333,6 +333,20 @@ __device__ void load_twiddles(C* dst, const C* src, int twlog)
 {
     for (int k = threadIdx.x; k < (1 << (twlog - 1)); k += blockDim.x)
         dst[k] = src[k];
+}
+
+// Stage-packed twiddles for fft_passes of length 2^logn (2^logn - 1 entries):
+// stage s keeps exp(-2 pi i k / 2^s), k < 2^(s-1), at (2^(s-1) - 1) + k, so the
+// butterflies of a stage read consecutive entries (a table indexed k << (twlog
+// - s) puts a warp's reads 2^(twlog-s) entries apart, in one bank).
+template <typename C>
+__device__ void load_twiddles_packed(C* dst, const C* src, int logn, int twlog)
+{
+    for (int i = threadIdx.x; i < (1 << logn) - 1; i += blockDim.x) {
+        const int s = 32 - __clz(i + 1); // i + 1 in [2^(s-1), 2^s)
+        const int k = i + 1 - (1 << (s - 1));
+        dst[i] = src[k << (twlog - s)];
+    }
 }
 
 // --------------------------------------------------- bispectrum element index
