@@ -41,7 +41,7 @@
 // Out-of-range rows/columns are zero-filled by the TMA unit, which is exactly
 // the reference's guard (bispectrum.h:397-398): those triples add zero.  The
 // ring is refilled round robin: the warp that finishes iteration r, r % 16 ==
-// warp, issues iteration r + NS - kLag once every thread has released r - kLag.
+// warp, issues iteration r + NS - LAG once every thread has released r - LAG.
 //
 // Accumulation: plain FP32 within a batch (in registers), Kahan-compensated
 // across batches into (B, C) in HBM.  Every mbarrier wait is bounded.
@@ -54,7 +54,6 @@
 namespace smip_gpu {
 
 constexpr uint64_t kWaitNs = 2000000000ull; // 2 s
-constexpr int kLag = 2;                     // iterations between a stage's release and its refill
 
 template <int DE>
 struct BCfg {
@@ -80,9 +79,11 @@ struct BCfg {
     static constexpr int STAGE = AOFF + (FPS * ABYTES + 127) / 128 * 128;
     static constexpr int NSR = (200 * 1024) / STAGE;       // ~200 KB of frame stages
     static constexpr int NS = NSR > 16 ? 16 : (NSR < 4 ? 4 : NSR);
+    static constexpr int LAG = 2;                          // iterations between a stage's release and its refill
+                                                           // (3 at d = 32, with 6 stages, measured no faster)
     static constexpr int SMEM = NS * STAGE + 2 * NS * 8 + 16;
     static_assert(RPC * NLB * NJB == WARPS && ROWS % RPC == 0, "task split");
-    static_assert(BW <= 256 && NS > kLag + 1 && SMEM <= 227 * 1024, "box / ring");
+    static_assert(BW <= 256 && NS > LAG + 1 && SMEM <= 227 * 1024, "box / ring");
 };
 
 struct BispecArgs {
@@ -228,9 +229,9 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
         }
     };
 
-    // The first NS - kLag iterations are issued up front; afterwards the warp
-    // that finishes iteration r with r % WARPS == warp issues r + NS - kLag.
-    constexpr uint32_t kAhead = Cf::NS - kLag;
+    // The first NS - LAG iterations are issued up front; afterwards the warp
+    // that finishes iteration r with r % WARPS == warp issues r + NS - LAG.
+    constexpr uint32_t kAhead = Cf::NS - Cf::LAG;
     if (threadIdx.x == 0) {
         const TileInfo ti = decode_tile<DE>(split_unit ? split_tile() : (int)blockIdx.x, p);
         s_box[0] = (ti.j0 + half_h - DE / 2) & ~1;
@@ -342,8 +343,8 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
                 if (!stop && nr < niter) {
                     bool go = true;
                     if (lane == 0) {
-                        const uint32_t prev = r - kLag; // the iteration that last used the stage
-                        if (r >= (uint32_t)kLag
+                        const uint32_t prev = r - Cf::LAG; // the iteration that last used the stage
+                        if (r >= (uint32_t)Cf::LAG
                             && !mbar_wait_bounded(&empty[prev % Cf::NS], (prev / Cf::NS) & 1, kWaitNs)) {
                             record_error(p.err, SMIP_DEV_ERR_TIMEOUT);
                             go = false;
@@ -590,12 +591,14 @@ cudaError_t launch_bispec_accumulate(const BispecLaunch& L, const Geometry& g, c
 }
 
 // ------------------------------------------------------- normalise, merge
-__global__ void bispec_normalize_kernel(const float2* __restrict__ B, const float2* __restrict__ C, double n,
+// (B - C) / n: the difference is exact in FP64; a multiply by 1/n instead of
+// a divide keeps the FP64 pipe's share small (GB300's FP64 rate is low).
+__global__ void bispec_normalize_kernel(const float2* __restrict__ B, const float2* __restrict__ C, double inv_n,
                                         long long count, float2* __restrict__ out)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x) {
         const float2 b = B[i], c = C[i];
-        out[i] = make_float2((float)(((double)b.x - (double)c.x) / n), (float)(((double)b.y - (double)c.y) / n));
+        out[i] = make_float2((float)(((double)b.x - (double)c.x) * inv_n), (float)(((double)b.y - (double)c.y) * inv_n));
     }
 }
 
@@ -619,7 +622,7 @@ __global__ void bispec_merge_kernel(float2* __restrict__ Bd, float2* __restrict_
 cudaError_t launch_bispec_normalize(const float2* B, const float2* C, double nframes, long long n, float2* out,
                                     cudaStream_t st)
 {
-    bispec_normalize_kernel<<<2048, 256, 0, st>>>(B, C, nframes, n, out); note_launches(1);
+    bispec_normalize_kernel<<<2048, 256, 0, st>>>(B, C, 1.0 / nframes, n, out); note_launches(1);
     return cudaGetLastError();
 }
 

@@ -77,11 +77,14 @@ __global__ void __launch_bounds__(256) fft_lines_d_kernel(double2* __restrict__ 
     }
 }
 
+// max |Z| over the grid: per-block maxima combined with an integer atomicMax
+// on the bit patterns (non-negative doubles order like their bits), so the
+// result does not depend on block order; *out must be zero beforehand.
 __global__ void max_abs_kernel(const double2* __restrict__ Z, int n, double* out)
 {
     __shared__ double red[32];
     double m = 0.0;
-    for (int p = threadIdx.x; p < n; p += blockDim.x) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
         const double2 z = Z[p];
         m = fmax(m, hypot(z.x, z.y));
     }
@@ -95,7 +98,7 @@ __global__ void max_abs_kernel(const double2* __restrict__ Z, int n, double* out
         double r = red[0];
         for (int i = 1; i < (int)(blockDim.x >> 5); ++i)
             r = fmax(r, red[i]);
-        *out = r;
+        atomicMax(reinterpret_cast<unsigned long long*>(out), (unsigned long long)__double_as_longlong(r));
     }
 }
 
@@ -123,7 +126,9 @@ cudaError_t launch_finish(const double* Phalf, double pnorm, const double2* phas
     // FFTW_BACKWARD over rows (x) then columns (y)
     fft_lines_d_kernel<<<(g.H + 3) / 4, 256, smem, st>>>(Z, g.logW, g.H, g.W, 1, +1, tw64); note_launches(1);
     fft_lines_d_kernel<<<(g.W + 3) / 4, 256, smem, st>>>(Z, g.logH, g.W, 1, g.W, +1, tw64); note_launches(1);
-    max_abs_kernel<<<1, 1024, 0, st>>>(Z, n, maxbuf); note_launches(1);
+    if ((e = cudaMemsetAsync(maxbuf, 0, sizeof(double), st)) != cudaSuccess)
+        return e;
+    max_abs_kernel<<<(n + 255) / 256 < 256 ? (n + 255) / 256 : 256, 256, 0, st>>>(Z, n, maxbuf); note_launches(1);
     scale_kernel<<<grid_n(n), 256, 0, st>>>(Z, n, maxbuf); note_launches(1);
     return cudaGetLastError();
 }
