@@ -16,6 +16,10 @@ latency (p50/p99).
             (host->device copies in the timed region), shifts read back
   --impl reference -- the CPU oracle (plain-C port of the reference's hot
             path) on the host cores, all threads, a bounded sample per step.
+  --workload binary128 | extended512 -- the other single-stack configurations
+            (40 x 128x128 u8 binary star, -b 32 -p 64; 10000 x 512x512 u16,
+            -b 48 -p 200, --nframes bounds the stack); stacks smaller than
+            L2 are timed step by step with an L2 flush between steps.
 
 Multi-GPU (torchrun): every rank processes its own stack (replicas, no
 collective on the data path); value = all frames / max rank time.
@@ -144,6 +148,15 @@ def fp32_peak_tflops(torch, dev):
     return best
 
 
+L2_BYTES = 129 * 2 ** 20
+
+
+def workload_desc(name, spec, nf):
+    obj = "binary star" if spec.kind == "binary" else "extended object"
+    return (f"{name}: {nf} x {spec.n}x{spec.n} {'u8' if spec.dtype == 'uint8' else 'u16'} {obj}, "
+            f"D/r0={spec.d_over_r0:g}, bdepth {spec.bdepth}, reco radius {spec.reco_radius:g}")
+
+
 def cpu_baseline(frames, depth, budget_s=12.0, threads=None):
     """The CPU oracle (plain-C port of the reference's per-frame path) on the
     host cores: frames/s over a bounded sample of the same stack."""
@@ -163,8 +176,8 @@ def cpu_baseline(frames, depth, budget_s=12.0, threads=None):
         done += 1
     el = time.perf_counter() - t0
     return {"value": done / el, "unit": "frames/s", "cores": threads, "kind": "port",
-            "sample": f"{done} frames of the {n}x{n} u16 stack (FFT, shift-and-add, power, bispectrum d={depth}), "
-                      f"{el:.1f} s"}
+            "sample": f"{done} frames of the {n}x{n} {frames.dtype} stack (FFT, shift-and-add, power, "
+                      f"bispectrum d={depth}), {el:.1f} s"}
 
 
 def run_reference(args):
@@ -173,7 +186,7 @@ def run_reference(args):
         return
     from smip_gb300 import synthetic as S
 
-    spec = S.config_spec(WORKLOAD)
+    spec = S.config_spec(args.workload)
     per_step = 64
     frames = S.make_stack(spec, 0, per_step * (args.steps + args.warmup))
     threads = os.cpu_count() or 1
@@ -198,10 +211,10 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded speckle frames)",
-        "config": {"workload": f"{WORKLOAD}: 2000 x 256x256 u16, bdepth 32, reco radius 128",
+        "config": {"workload": workload_desc(args.workload, spec, args.nframes or spec.nframes),
                    "per_step_sample": f"{per_step} frames"},
         "cpu_baseline": {"value": value, "unit": "frames/s", "cores": threads, "kind": "port",
-                         "sample": f"{per_step} frames per step of the 256x256 u16 stack; plain-C port of "
+                         "sample": f"{per_step} frames per step of the {spec.n}x{spec.n} stack; plain-C port of "
                                    "the reference's per-frame path (oracle/smip_oracle.c)"},
         "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -262,13 +275,15 @@ def run_ours(args):
     from smip_gb300 import synthetic as S
     from smip_gb300.distributed import replica_seed
 
-    spec = S.config_spec(WORKLOAD, nframes=args.nframes, seed=replica_seed(2000, rank))
+    spec0 = S.config_spec(args.workload)
+    nf = args.nframes or spec0.nframes
+    spec = S.config_spec(args.workload, nframes=nf, seed=replica_seed(spec0.seed, rank))
     # frames first (spawn pool before any CUDA call)
     t_gen = time.perf_counter()
     procs = min(16, os.cpu_count() or 1)
-    frames = gen_frames(spec, args.nframes, procs)
+    frames = gen_frames(spec, nf, procs)
     serve_jobs = None
-    if rank == 0 and world == 1 and not args.no_serve:
+    if rank == 0 and world == 1 and not args.no_serve and args.workload == WORKLOAD:
         serve_jobs = make_serving_jobs(procs)
     t_gen = time.perf_counter() - t_gen
 
@@ -283,10 +298,17 @@ def run_ours(args):
     import smip_gb300 as G
 
     n, D, R = spec.n, spec.bdepth, float(spec.reco_radius)
-    nf = args.nframes
-    frames_dev = torch.from_numpy(frames.view(np.int16)).to(dev).view(torch.uint16)
-    pinned = torch.from_numpy(frames.view(np.int16)).pin_memory()
-    pinned_np = pinned.numpy().view(np.uint16)
+    if frames.dtype == np.uint16:
+        frames_dev = torch.from_numpy(frames.view(np.int16)).to(dev).view(torch.uint16)
+        pinned = torch.from_numpy(frames.view(np.int16)).pin_memory()
+        pinned_np = pinned.numpy().view(np.uint16)
+    else:
+        frames_dev = torch.from_numpy(frames).to(dev)
+        pinned = torch.from_numpy(frames).pin_memory()
+        pinned_np = pinned.numpy()
+    # stacks smaller than L2 are timed step by step, L2 flushed in between
+    small = frames.nbytes < 2 * L2_BYTES
+    flush = torch.empty(4 * L2_BYTES // 4, dtype=torch.float32, device=dev) if small else None
     stream = torch.cuda.Stream(device=dev)
     st = G.Stack(n, n, D, device=local, stream=stream.cuda_stream)
 
@@ -314,15 +336,29 @@ def run_ours(args):
     launches0 = G.kernel_launches()
     barrier()
     with ClockSampler(local) as clk:
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            step_dev()
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
+        if not small:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                step_dev()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            el_dev = e0.elapsed_time(e1) * 1e-3
+        else:
+            el_dev = 0.0
+            for _ in range(args.steps):
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                step_dev()
+                e1.record(stream)
+                torch.cuda.synchronize(dev)
+                el_dev += e0.elapsed_time(e1) * 1e-3
     launches = G.kernel_launches() - launches0
-    elapsed = max_over_ranks(e0.elapsed_time(e1) * 1e-3)
+    elapsed = max_over_ranks(el_dev)
     k2_ms, k2_n, k2_frames = st.kernel_time()
     st.set_timing(False)
     clocks = clk.summary()
@@ -362,7 +398,7 @@ def run_ours(args):
     # spectra part, scaled to this run's frames per launch
     traffic = None
     prof = os.path.join(ROOT, "profiles", "bispec_accum_extended256.txt")
-    if os.path.exists(prof) and k2_n:
+    if os.path.exists(prof) and k2_n and args.workload == WORKLOAD:
         kv = {}
         for line in open(prof):
             if ":" in line and line.split(":")[0].startswith("dram_bytes_"):
@@ -371,7 +407,7 @@ def run_ours(args):
             traffic = kv["dram_bytes_fixed_per_launch"] + kv["dram_bytes_per_frame"] * (k2_frames / k2_n)
     roofline = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                "kernel": "bispec_accum_kernel<32>", "launches": k2_n,
+                "kernel": f"bispec_accum_kernel<{(D // 2 * 2 + 7) // 8 * 8}>", "launches": k2_n,
                 "avg_launch_ms": k2_ms / max(k2_n, 1), "frames_per_launch": k2_frames / max(k2_n, 1),
                 "algorithmic": f"14 FLOP x {T} triples per frame",
                 "peak_source": "cuBLAS FP32 SGEMM 8192^3, TF32 off, measured in this run"}
@@ -384,8 +420,10 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 phase recursion)",
         "data": "synthetic (seeded speckle frames, Kolmogorov PSFs)",
-        "config": {"workload": f"{WORKLOAD}: {nf} x 256x256 u16 extended object, D/r0=15, bdepth 32, reco radius 128",
-                   "frames_per_step_per_gpu": nf, "l2": "inputs larger than L2 (262 MB frames per step)",
+        "config": {"workload": workload_desc(args.workload, spec, nf),
+                   "frames_per_step_per_gpu": nf,
+                   "l2": (f"L2 flushed between steps ({frames.nbytes / 1e6:.1f} MB frames per step)" if small else
+                          f"inputs larger than L2 ({frames.nbytes / 1e6:.0f} MB frames per step)"),
                    "parallelism": f"replicas x{world}", "batch_frames": None},
         "e2e": e2e, "gpu_launches": launches, "roofline": roofline, "cpu_baseline": cpu,
         "clocks": clocks, "recon_latency": recon,
@@ -407,7 +445,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--nframes", type=int, default=2000)
+    ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "binary128", "extended512"])
+    ap.add_argument("--nframes", type=int, default=None, help="frames of the stack (default: the workload's own)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the batched and served measurements")
     args = ap.parse_args()
