@@ -307,7 +307,7 @@ def run_ours(args):
         pinned = torch.from_numpy(frames).pin_memory()
         pinned_np = pinned.numpy()
     # stacks smaller than L2 are timed step by step, L2 flushed in between
-    small = frames.nbytes < 2 * L2_BYTES
+    small = frames.nbytes < L2_BYTES
     flush = torch.empty(4 * L2_BYTES // 4, dtype=torch.float32, device=dev) if small else None
     stream = torch.cuda.Stream(device=dev)
     st = G.Stack(n, n, D, device=local, stream=stream.cuda_stream)
