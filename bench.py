@@ -250,18 +250,26 @@ def serving_metrics(jobs):
     for key, jl, realtime, desc in (("batched", batched, False, BATCHED_DESC), ("served", served, True, SERVED_DESC)):
         eng = serve.Engine(budget_bytes=120e9, max_active=64, workers=32)
         eng.prewarm(shapes, count=24)
+        eng_g = serve.Engine(budget_bytes=120e9, max_active=64, workers=32, graph=True)
+        eng_g.prewarm(shapes, count=24)
         serve.run_plain(jl[:3], realtime=False)  # warm the code paths
+        eng_g.run(jl[:8], realtime=False)
         # best of two runs of each (host thread scheduling varies run to run)
         runs_s = [eng.run(jl, realtime=realtime) for _ in range(2)]
+        runs_g = [eng_g.run(jl, realtime=realtime) for _ in range(2)]
         runs_p = [serve.run_plain(jl, realtime=realtime) for _ in range(2)]
         res_s, span_s = min(runs_s, key=lambda x: x[1])
+        res_g, span_g = min(runs_g, key=lambda x: x[1])
         res_p, span_p = min(runs_p, key=lambda x: x[1])
         s, p = serve.summarize(res_s, span_s), serve.summarize(res_p, span_p)
+        sg = serve.summarize(res_g, span_g)
         out[key] = {"workload": desc, "served": s, "plain": p,
                     "frames_per_s_ratio": s["frames_per_s"] / p["frames_per_s"],
                     "results_identical": serve.compare_results(res_s, res_p),
-                    "peak_jobs_in_flight": eng.peak_active}
-        del eng
+                    "peak_jobs_in_flight": eng.peak_active,
+                    "served_graph": sg, "frames_per_s_ratio_graph": sg["frames_per_s"] / p["frames_per_s"],
+                    "results_identical_graph": serve.compare_results(res_g, res_p)}
+        del eng, eng_g
     del keep
     return out
 

@@ -108,6 +108,15 @@ SMIP_GPU_API int smip_stack_reset(smip_stack_t s);
 SMIP_GPU_API int smip_stack_flush(smip_stack_t s);
 SMIP_GPU_API int smip_stack_sync(smip_stack_t s);
 
+/* Runs the pending (staged, not yet launched) frame batches of count stacks
+ * as one CUDA graph: one branch per stack, the branches concurrent.  Stacks
+ * without pending frames are skipped; all must live on one device and appear
+ * once.  Later calls on each stack are ordered after the graph.  The results
+ * are those of smip_stack_flush on each stack.  No counterpart in the
+ * reference, which accumulates one stack per smip-cli run (main.cpp:281-312);
+ * this is the graph-captured many-stack launch the serving loop uses. */
+SMIP_GPU_API int smip_batch_launch(smip_stack_t* stacks, long count);
+
 SMIP_GPU_API int smip_stack_frame_count(smip_stack_t s, long* nframes);
 SMIP_GPU_API int smip_stack_bispectrum_size(smip_stack_t s, long* base_size);
 

@@ -19,6 +19,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <map>
 #include <mutex>
 #include <string>
@@ -70,6 +71,12 @@ struct DeviceCtx {
     double2* tw64 = nullptr;
     dfc* twdf = nullptr;     // the same table as float-float (hi, lo)
     int num_sms = 0;
+    // smip_batch_launch: the stream the graphs launch on, its fork/done
+    // events and the executable graph of the last call (updated in place)
+    std::shared_ptr<std::mutex> gmu = std::make_shared<std::mutex>();
+    cudaStream_t gst = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
+    cudaGraphExec_t gexec = nullptr;
 };
 
 std::mutex g_ctx_mu;
@@ -340,12 +347,19 @@ struct smip_stack {
     double2* Z = nullptr;
     double* pfull = nullptr;
     double* maxbuf = nullptr;
+    // smip_batch_launch: this stack's branch of the graph is captured on bst
+    cudaStream_t bst = nullptr;
+    cudaEvent_t ev_join = nullptr, ev_dep = nullptr;
 
     ~smip_stack()
     {
         cudaSetDevice(device);
         if (st)
             cudaStreamSynchronize(st);
+        if (bst)
+            cudaStreamDestroy(bst);
+        if (ev_join) cudaEventDestroy(ev_join);
+        if (ev_dep) cudaEventDestroy(ev_dep);
         dfree(B); dfree(C); dfree(Bn); dfree(P); dfree(Ppart);
         if (sum) cudaFree(sum);
         if (cst)
@@ -442,48 +456,57 @@ struct smip_stack {
         cur = 0;
     }
 
-    int run_batch()
+    // Host-side preparation of the pending batch: every allocation and
+    // synchronisation happens here, so that issue_batch can be captured.
+    int prepare_batch()
     {
-        const int n = pending;
-        if (n == 0)
+        if (pending == 0)
             return SMIP_OK;
-        const long first_index = nframes - n;
-        if (mode == 2) {
-            CUDA_TRY(launch_import_spectra(spec_staging, n, g, S, st));
-        } else {
-            const size_t fe = frame_elems();
-            const bool first = !has_ref;
-            void* staging = stg[cur];
-            // the batch's frames are on the copy stream
-            CUDA_TRY(cudaEventRecord(ev_copied[cur], cst));
-            CUDA_TRY(cudaStreamWaitEvent(st, ev_copied[cur], 0));
+        if (mode != 2) {
             int rc = ensure_shift_cap(nframes);
             if (rc)
                 return rc;
-            if (first) {
-                CUDA_TRY(cudaMemcpyAsync(ref, staging, dtype_size(dtype) * fe, cudaMemcpyDeviceToDevice, st));
-                CUDA_TRY(launch_sumsq(dtype, ref, (long long)fe, ref_sq, st));
-            }
-            CUDA_TRY(launch_row_pass(dtype, staging, (long long)fe, n, g, Gt, ctx->twdf, st));
-            if (first)
-                CUDA_TRY(launch_col_pass(1, Gt, S, R, R, T, Ppart, 1, fpc, 0, g, ctx->twdf, ctx->tw32, st));
-            CUDA_TRY(launch_col_pass(0, Gt, S, R, nullptr, T, Ppart, n, fpc, first ? 1 : 0, g, ctx->twdf, ctx->tw32,
-                                     st));
-            CUDA_TRY(launch_power_reduce(P, Ppart, (n + fpc - 1) / fpc, g, st));
-            CUDA_TRY(launch_xcorr_rows(T, corr, n, g, ctx->tw32, st));
-            CUDA_TRY(launch_xcorr_shift(dtype, corr, staging, (long long)fe, ref, ref_sq, n, first ? 1 : 0, g,
-                                        shifts + 2 * first_index, st));
-            CUDA_TRY(launch_saa_add(dtype, sum, staging, (long long)fe, n, first ? 1 : 0, shifts + 2 * first_index, g, st));
-            // the last reader of this buffer; the copy stream refills it after this
-            CUDA_TRY(cudaEventRecord(ev_free[cur], st));
-            free_rec[cur] = true;
-            cur ^= 1;
-            has_ref = true;
         }
         if (!kscratch) {
             CUDA_TRY(cudaMalloc(&kscratch, bispec_scratch_bytes(ctx->num_sms)));
             CUDA_TRY(cudaMalloc(&ktile_cnt, sizeof(int) * ctx->num_sms));
             CUDA_TRY(cudaMemsetAsync(ktile_cnt, 0, sizeof(int) * ctx->num_sms, st));
+        }
+        return SMIP_OK;
+    }
+
+    // The pending batch's device work on stream q (kernels and device copies
+    // only).  wait_copies: order it after the batch's frame copies on cst
+    // (a graph launch orders them outside the graph instead).  timed: CUDA
+    // events around the bispectrum kernel.
+    int issue_batch(cudaStream_t q, bool wait_copies, bool timed)
+    {
+        const int n = pending;
+        const long first_index = nframes - n;
+        if (mode == 2) {
+            CUDA_TRY(launch_import_spectra(spec_staging, n, g, S, q));
+        } else {
+            const size_t fe = frame_elems();
+            const bool first = !has_ref;
+            void* staging = stg[cur];
+            if (wait_copies) {
+                CUDA_TRY(cudaEventRecord(ev_copied[cur], cst));
+                CUDA_TRY(cudaStreamWaitEvent(q, ev_copied[cur], 0));
+            }
+            if (first) {
+                CUDA_TRY(cudaMemcpyAsync(ref, staging, dtype_size(dtype) * fe, cudaMemcpyDeviceToDevice, q));
+                CUDA_TRY(launch_sumsq(dtype, ref, (long long)fe, ref_sq, q));
+            }
+            CUDA_TRY(launch_row_pass(dtype, staging, (long long)fe, n, g, Gt, ctx->twdf, q));
+            if (first)
+                CUDA_TRY(launch_col_pass(1, Gt, S, R, R, T, Ppart, 1, fpc, 0, g, ctx->twdf, ctx->tw32, q));
+            CUDA_TRY(launch_col_pass(0, Gt, S, R, nullptr, T, Ppart, n, fpc, first ? 1 : 0, g, ctx->twdf, ctx->tw32,
+                                     q));
+            CUDA_TRY(launch_power_reduce(P, Ppart, (n + fpc - 1) / fpc, g, q));
+            CUDA_TRY(launch_xcorr_rows(T, corr, n, g, ctx->tw32, q));
+            CUDA_TRY(launch_xcorr_shift(dtype, corr, staging, (long long)fe, ref, ref_sq, n, first ? 1 : 0, g,
+                                        shifts + 2 * first_index, q));
+            CUDA_TRY(launch_saa_add(dtype, sum, staging, (long long)fe, n, first ? 1 : 0, shifts + 2 * first_index, g, q));
         }
         BispecLaunch L;
         L.S = S;
@@ -494,7 +517,7 @@ struct smip_stack {
         L.num_sms = ctx->num_sms;
         L.scratch = kscratch;
         L.tile_cnt = ktile_cnt;
-        if (timing) {
+        if (timed) {
             if (ev_used == ev_pool.size()) {
                 cudaEvent_t a, b;
                 CUDA_TRY(cudaEventCreate(&a));
@@ -502,15 +525,39 @@ struct smip_stack {
                 ev_pool.emplace_back(a, b);
                 ev_frames.push_back(0);
             }
-            CUDA_TRY(cudaEventRecord(ev_pool[ev_used].first, st));
+            CUDA_TRY(cudaEventRecord(ev_pool[ev_used].first, q));
         }
-        CUDA_TRY(launch_bispec_accumulate(L, g, st));
-        if (timing) {
-            CUDA_TRY(cudaEventRecord(ev_pool[ev_used].second, st));
+        CUDA_TRY(launch_bispec_accumulate(L, g, q));
+        if (timed) {
+            CUDA_TRY(cudaEventRecord(ev_pool[ev_used].second, q));
             ev_frames[ev_used] = n;
             ++ev_used;
         }
+        return SMIP_OK;
+    }
+
+    // Host bookkeeping once the batch's work is issued and ev_free[cur] is
+    // recorded after its last read of the frame buffer.
+    void commit_batch()
+    {
+        if (mode != 2) {
+            free_rec[cur] = true; // the copy stream refills this buffer after ev_free[cur]
+            cur ^= 1;
+            has_ref = true;
+        }
         pending = 0;
+    }
+
+    int run_batch()
+    {
+        if (pending == 0)
+            return SMIP_OK;
+        int rc = prepare_batch();
+        if (rc || (rc = issue_batch(st, true, timing)))
+            return rc;
+        if (mode != 2)
+            CUDA_TRY(cudaEventRecord(ev_free[cur], st)); // the last reader of this buffer
+        commit_batch();
         return SMIP_OK;
     }
 
@@ -748,6 +795,107 @@ extern "C" int smip_stack_sync(smip_stack_t s)
     if (rc)
         return rc;
     return check_dev_err(s->err, s->st);
+}
+
+// One CUDA graph for the pending batches of several stacks: each stack's
+// kernels form one branch, captured on the stack's own capture stream
+// between a fork and a join on the device's graph stream, so the branches
+// run concurrently.  The executable graph of the previous call is updated
+// in place when the new graph has the same topology.
+extern "C" int smip_batch_launch(smip_stack_t* stacks, long count)
+{
+    if (count < 0 || (count > 0 && !stacks))
+        return fail(SMIP_E_INVALID_ARGUMENT, "invalid stack list");
+    std::vector<smip_stack*> L;
+    for (long i = 0; i < count; ++i) {
+        int rc = check_stack(stacks[i]);
+        if (rc)
+            return rc;
+        if (stacks[i]->device != stacks[0]->device)
+            return fail(SMIP_E_INVALID_ARGUMENT, "stacks must live on the same device");
+        if (std::find(L.begin(), L.end(), stacks[i]) != L.end())
+            return fail(SMIP_E_INVALID_ARGUMENT, "a stack appears twice in the list");
+        if (stacks[i]->pending > 0)
+            L.push_back(stacks[i]);
+    }
+    if (L.empty())
+        return SMIP_OK;
+    DeviceCtx* ctx = L[0]->ctx;
+    std::lock_guard<std::mutex> lk(*ctx->gmu);
+    CUDA_TRY(cudaSetDevice(L[0]->device));
+    if (!ctx->gst) {
+        CUDA_TRY(cudaStreamCreateWithFlags(&ctx->gst, cudaStreamNonBlocking));
+        CUDA_TRY(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+        CUDA_TRY(cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming));
+    }
+    cudaStream_t G = ctx->gst;
+    for (smip_stack* s : L) {
+        int rc = s->prepare_batch();
+        if (rc)
+            return rc;
+        if (!s->bst) {
+            CUDA_TRY(cudaStreamCreateWithFlags(&s->bst, cudaStreamNonBlocking));
+            CUDA_TRY(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+            CUDA_TRY(cudaEventCreateWithFlags(&s->ev_dep, cudaEventDisableTiming));
+        }
+        // the graph runs after the stack's earlier work and its batch's frame copies
+        CUDA_TRY(cudaEventRecord(s->ev_dep, s->st));
+        CUDA_TRY(cudaStreamWaitEvent(G, s->ev_dep, 0));
+        if (s->mode != 2) {
+            CUDA_TRY(cudaEventRecord(s->ev_copied[s->cur], s->cst));
+            CUDA_TRY(cudaStreamWaitEvent(G, s->ev_copied[s->cur], 0));
+        }
+    }
+    CUDA_TRY(cudaStreamBeginCapture(G, cudaStreamCaptureModeRelaxed));
+    int rc = SMIP_OK;
+    cudaError_t ce = cudaEventRecord(ctx->ev_fork, G);
+    for (size_t i = 0; i < L.size() && ce == cudaSuccess && rc == SMIP_OK; ++i) {
+        smip_stack* s = L[i];
+        ce = cudaStreamWaitEvent(s->bst, ctx->ev_fork, 0);
+        if (ce == cudaSuccess)
+            rc = s->issue_batch(s->bst, false, false);
+        if (ce == cudaSuccess && rc == SMIP_OK)
+            ce = cudaEventRecord(s->ev_join, s->bst);
+        if (ce == cudaSuccess && rc == SMIP_OK)
+            ce = cudaStreamWaitEvent(G, s->ev_join, 0);
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(G, &graph);
+    if (rc != SMIP_OK || ce != cudaSuccess || ee != cudaSuccess) {
+        if (graph)
+            cudaGraphDestroy(graph);
+        cudaGetLastError();
+        if (rc != SMIP_OK)
+            return rc;
+        return fail(SMIP_E_CUDA, cudaGetErrorString(ce != cudaSuccess ? ce : ee));
+    }
+    bool updated = false;
+    if (ctx->gexec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(ctx->gexec, graph, &info) == cudaSuccess) {
+            updated = true;
+        } else {
+            cudaGetLastError();
+            cudaGraphExecDestroy(ctx->gexec); // freed once a launch still in flight completes
+            ctx->gexec = nullptr;
+        }
+    }
+    cudaError_t ie = updated ? cudaSuccess : cudaGraphInstantiate(&ctx->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+        ctx->gexec = nullptr;
+        return fail(SMIP_E_CUDA, cudaGetErrorString(ie));
+    }
+    CUDA_TRY(cudaGraphLaunch(ctx->gexec, G));
+    CUDA_TRY(cudaEventRecord(ctx->ev_done, G));
+    for (smip_stack* s : L) {
+        // later work on the stack's stream, and the refill of its frame buffer, follow the graph
+        CUDA_TRY(cudaStreamWaitEvent(s->st, ctx->ev_done, 0));
+        if (s->mode != 2)
+            CUDA_TRY(cudaEventRecord(s->ev_free[s->cur], G));
+        s->commit_batch();
+    }
+    return SMIP_OK;
 }
 
 extern "C" int smip_stack_frame_count(smip_stack_t s, long* n)

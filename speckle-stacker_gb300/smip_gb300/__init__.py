@@ -103,6 +103,7 @@ def _load():
         "smip_stack_reconstruct": ([vp, C.c_double, dp, ubp, dp], C.c_int),
         "smip_stack_finish": ([vp, C.c_double, dp, dp, ubp, dp], C.c_int),
         "smip_stack_merge": ([vp, vp], C.c_int),
+        "smip_batch_launch": ([C.POINTER(vp), C.c_long], C.c_int),
         "smip_stack_share_reference": ([vp, vp], C.c_int),
         "smip_stack_save_bispectrum": ([vp, C.c_char_p], C.c_int),
         "smip_stack_load_bispectrum": ([vp, C.c_char_p, C.c_long], C.c_int),
@@ -151,6 +152,15 @@ def version():
     a, b, c = C.c_int(), C.c_int(), C.c_int()
     _check(_L().smip_version(C.byref(a), C.byref(b), C.byref(c)))
     return a.value, b.value, c.value
+
+
+def batch_launch(stacks) -> None:
+    """Runs the pending frame batches of ``stacks`` as one CUDA graph launch
+    (one concurrent branch per stack); stacks without pending frames are
+    skipped.  Later calls on each stack are ordered after the graph."""
+    stacks = list(stacks)
+    arr = (C.c_void_p * max(1, len(stacks)))(*[st._h.value for st in stacks])
+    _check(_L().smip_batch_launch(arr, len(stacks)))
 
 
 def kernel_launches() -> int:

@@ -116,16 +116,24 @@ class Engine:
     max_active: jobs in flight at once (streaming or reconstructing).
     workers: threads that run phase recovery + the final image.
     stack_factory: (ncols, nrows, bdepth) -> stack; defaults to smip_gb300.Stack.
+    graph: the last batches of the jobs whose frames are all in after a round
+        run as one CUDA graph launch (smip_gb300.batch_launch) before their
+        reconstructions start, instead of one flush per job.
     """
 
     def __init__(self, device: int = 0, budget_bytes: float = 120e9, max_active: int = 64, workers: int = 32,
-                 stack_factory: Optional[Callable] = None):
+                 stack_factory: Optional[Callable] = None, graph: bool = False,
+                 batch_launch: Optional[Callable] = None):
         if stack_factory is None:
             from smip_gb300 import Stack
 
             def stack_factory(nc, nr, d):
                 return Stack(nc, nr, d, device=device)
+        if graph and batch_launch is None:
+            from smip_gb300 import batch_launch
         self.factory = stack_factory
+        self.graph = bool(graph)
+        self.batch_launch = batch_launch
         self.budget = float(budget_bytes)
         self.max_active = int(max_active)
         self.workers = int(workers)
@@ -182,6 +190,7 @@ class Engine:
                 self.peak_active = max(self.peak_active, len(active) + len(running))
                 # one chunk per streaming job, round robin
                 pushed = False
+                ready = []
                 for entry in list(active):
                     job, st, pos = entry[0], entry[1], entry[2]
                     k = min(job.chunk, len(job.frames) - pos)
@@ -191,8 +200,12 @@ class Engine:
                     pushed = True
                     if entry[2] == len(job.frames):
                         active.remove(entry)
-                        fut = ex.submit(self._finish, job, st, t0, entry[3])
-                        running[fut] = (job, st, entry[4])
+                        ready.append(entry)
+                if self.graph and ready:
+                    self.batch_launch([e[1] for e in ready])
+                for entry in ready:
+                    fut = ex.submit(self._finish, entry[0], entry[1], t0, entry[3])
+                    running[fut] = (entry[0], entry[1], entry[4])
                 # completions
                 done = [f for f in running if f.done()]
                 for f in done:

@@ -67,6 +67,22 @@ def test_engine_admission_and_results():
     assert s["jobs"] == 20 and s["frames"] == sum(len(j.frames) for j in jobs)
 
 
+def test_engine_graph_mode_launches_each_finished_job_once():
+    """With graph=True the stacks of the jobs whose frames are all in after a
+    round are handed to one batch launch before their reconstructions."""
+    jobs = _jobs(12)
+    calls = []
+
+    def launch(stacks):
+        assert all(len(st.frames) for st in stacks)  # every one holds its job's frames
+        calls.append([id(st) for st in stacks])
+
+    eng = serve.Engine(max_active=5, workers=2, stack_factory=FakeStack, graph=True, batch_launch=launch)
+    res, _ = eng.run(jobs, realtime=False)
+    assert sorted(r.id for r in res) == list(range(12))
+    assert sum(len(c) for c in calls) == 12 and all(len(set(c)) == len(c) for c in calls)
+
+
 def test_engine_realtime_respects_arrivals():
     jobs = _jobs(8, rate=200.0)
     eng = serve.Engine(max_active=4, workers=2, stack_factory=FakeStack)
@@ -90,18 +106,19 @@ def test_results_same_alone_and_in_mix(smip):
     """Jobs of mixed sizes (64^2 binary u8, 128^2 extended u16, uneven counts)
     served concurrently give exactly the results each gives alone."""
     jobs = serve.make_jobs(6, sizes=(64, 128), counts=(30, 300), bank_frames=64, seed=11)
-    eng = serve.Engine(max_active=6, workers=3)
-    eng.prewarm({j.shape for j in jobs}, count=3)
-    mixed, _ = eng.run(jobs, realtime=False)
     alone, _ = serve.run_plain(jobs, realtime=False)
     by_id = {r.id: r for r in alone}
-    assert eng.peak_active >= 2
-    for r in mixed:
-        a = by_id[r.id]
-        assert np.array_equal(r.shifts, a.shifts)
-        assert np.array_equal(r.flags, a.flags)
-        assert np.array_equal(r.phases, a.phases)
-        assert np.array_equal(r.image, a.image)
+    for graph in (False, True):  # last batches flushed per job, or one CUDA graph per round
+        eng = serve.Engine(max_active=6, workers=3, graph=graph)
+        eng.prewarm({j.shape for j in jobs}, count=3)
+        mixed, _ = eng.run(jobs, realtime=False)
+        assert eng.peak_active >= 2
+        for r in mixed:
+            a = by_id[r.id]
+            assert np.array_equal(r.shifts, a.shifts)
+            assert np.array_equal(r.flags, a.flags)
+            assert np.array_equal(r.phases, a.phases)
+            assert np.array_equal(r.image, a.image)
 
 
 def test_autotune_cache_roundtrip(tmp_path, monkeypatch):
@@ -146,3 +163,40 @@ def test_autotune_on_device(smip, tmp_path, monkeypatch):
         from conftest import rel_l2
 
         assert rel_l2(a.bispectrum(), b.bispectrum()) <= 1e-6
+
+
+@pytest.mark.gpu
+def test_batch_launch_matches_flush(smip):
+    """One CUDA graph over the pending batches of several stacks (uneven
+    shapes, depths and counts; some batches already launched on their own)
+    gives bit-identical results to flushing each stack, also when the graph
+    of the previous call is updated in place."""
+    rng = np.random.default_rng(5)
+    cfg = [(64, 16, 50), (128, 24, 130), (64, 16, 70), (256, 32, 40), (64, 16, 64)]
+    frames = [rng.integers(0, 4096, (nf, n, n)).astype(np.uint16) for n, d, nf in cfg]
+
+    def results(st):
+        return st.shifts(), st.sum(), st.power(), st.bispectrum()
+
+    def run(graph):
+        stacks = [smip.Stack(n, n, d, batch_frames=64) for n, d, _ in cfg]
+        out = []
+        for rnd in range(2):
+            for st, fr in zip(stacks, frames):
+                st.reset()
+                st.push_frames(fr[rnd:])  # 64 frames run as a batch during the push
+            if graph:
+                smip.batch_launch(stacks)
+            out.append([results(st) for st in stacks])
+        for st in stacks:
+            st.close()
+        return out
+
+    eager, graphed = run(False), run(True)
+    for re, rg in zip(eager, graphed):
+        for a, b in zip(re, rg):
+            for x, y in zip(a, b):
+                assert np.array_equal(x, y)
+    with smip.Stack(64, 64, 16) as st, pytest.raises(smip.InvalidArgument):
+        st.push_frames(frames[0][:3])
+        smip.batch_launch([st, st])
