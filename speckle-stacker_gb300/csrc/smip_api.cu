@@ -71,12 +71,18 @@ struct DeviceCtx {
     double2* tw64 = nullptr;
     dfc* twdf = nullptr;     // the same table as float-float (hi, lo)
     int num_sms = 0;
-    // smip_batch_launch: the stream the graphs launch on, its fork/done
-    // events and the executable graph of the last call (updated in place)
+    // smip_batch_launch: the streams the graphs launch on (round robin, so
+    // that consecutive calls' graphs overlap), their done events, the fork
+    // event of the capture, and executable graphs by topology (updated in
+    // place for a new call of the same topology)
+    static constexpr int kGraphStreams = 8;
     std::shared_ptr<std::mutex> gmu = std::make_shared<std::mutex>();
-    cudaStream_t gst = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_done = nullptr;
-    cudaGraphExec_t gexec = nullptr;
+    cudaStream_t gst[kGraphStreams] = {};
+    cudaEvent_t ev_done[kGraphStreams] = {};
+    int gnext = 0;
+    cudaEvent_t ev_fork = nullptr;
+    std::shared_ptr<std::map<std::vector<int>, cudaGraphExec_t>> gexec =
+        std::make_shared<std::map<std::vector<int>, cudaGraphExec_t>>();
 };
 
 std::mutex g_ctx_mu;
@@ -799,9 +805,9 @@ extern "C" int smip_stack_sync(smip_stack_t s)
 
 // One CUDA graph for the pending batches of several stacks: each stack's
 // kernels form one branch, captured on the stack's own capture stream
-// between a fork and a join on the device's graph stream, so the branches
-// run concurrently.  The executable graph of the previous call is updated
-// in place when the new graph has the same topology.
+// between a fork and a join on one of the device's graph streams, so the
+// branches run concurrently.  Executable graphs are kept by topology and
+// updated in place for a later call of the same topology.
 extern "C" int smip_batch_launch(smip_stack_t* stacks, long count)
 {
     if (count < 0 || (count > 0 && !stacks))
@@ -823,12 +829,22 @@ extern "C" int smip_batch_launch(smip_stack_t* stacks, long count)
     DeviceCtx* ctx = L[0]->ctx;
     std::lock_guard<std::mutex> lk(*ctx->gmu);
     CUDA_TRY(cudaSetDevice(L[0]->device));
-    if (!ctx->gst) {
-        CUDA_TRY(cudaStreamCreateWithFlags(&ctx->gst, cudaStreamNonBlocking));
+    if (!ctx->ev_fork) {
         CUDA_TRY(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
-        CUDA_TRY(cudaEventCreateWithFlags(&ctx->ev_done, cudaEventDisableTiming));
+        for (int k = 0; k < DeviceCtx::kGraphStreams; ++k) {
+            CUDA_TRY(cudaStreamCreateWithFlags(&ctx->gst[k], cudaStreamNonBlocking));
+            CUDA_TRY(cudaEventCreateWithFlags(&ctx->ev_done[k], cudaEventDisableTiming));
+        }
     }
-    cudaStream_t G = ctx->gst;
+    const int gk = ctx->gnext;
+    ctx->gnext = (gk + 1) % DeviceCtx::kGraphStreams;
+    cudaStream_t G = ctx->gst[gk];
+    // the graph's topology: per branch, frames or spectra and whether it
+    // holds the stack's first batch (reference frame work); and the graph
+    // stream, since launches of one executable graph run one after another
+    std::vector<int> topo { gk };
+    for (smip_stack* s : L)
+        topo.push_back(s->mode == 2 ? 2 : (s->has_ref ? 1 : 3));
     for (smip_stack* s : L) {
         int rc = s->prepare_batch();
         if (rc)
@@ -869,28 +885,38 @@ extern "C" int smip_batch_launch(smip_stack_t* stacks, long count)
             return rc;
         return fail(SMIP_E_CUDA, cudaGetErrorString(ce != cudaSuccess ? ce : ee));
     }
-    bool updated = false;
-    if (ctx->gexec) {
+    auto& cache = *ctx->gexec;
+    cudaGraphExec_t exec = nullptr;
+    auto it = cache.find(topo);
+    if (it != cache.end()) {
         cudaGraphExecUpdateResultInfo info;
-        if (cudaGraphExecUpdate(ctx->gexec, graph, &info) == cudaSuccess) {
-            updated = true;
+        if (cudaGraphExecUpdate(it->second, graph, &info) == cudaSuccess) {
+            exec = it->second;
         } else {
             cudaGetLastError();
-            cudaGraphExecDestroy(ctx->gexec); // freed once a launch still in flight completes
-            ctx->gexec = nullptr;
+            cudaGraphExecDestroy(it->second); // freed once a launch still in flight completes
+            cache.erase(it);
         }
     }
-    cudaError_t ie = updated ? cudaSuccess : cudaGraphInstantiate(&ctx->gexec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ie != cudaSuccess) {
-        ctx->gexec = nullptr;
-        return fail(SMIP_E_CUDA, cudaGetErrorString(ie));
+    if (!exec) {
+        if (cache.size() >= 64) { // bounded: drop them all
+            for (auto& e : cache)
+                cudaGraphExecDestroy(e.second);
+            cache.clear();
+        }
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        if (ie != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            return fail(SMIP_E_CUDA, cudaGetErrorString(ie));
+        }
+        cache[topo] = exec;
     }
-    CUDA_TRY(cudaGraphLaunch(ctx->gexec, G));
-    CUDA_TRY(cudaEventRecord(ctx->ev_done, G));
+    cudaGraphDestroy(graph);
+    CUDA_TRY(cudaGraphLaunch(exec, G));
+    CUDA_TRY(cudaEventRecord(ctx->ev_done[gk], G));
     for (smip_stack* s : L) {
         // later work on the stack's stream, and the refill of its frame buffer, follow the graph
-        CUDA_TRY(cudaStreamWaitEvent(s->st, ctx->ev_done, 0));
+        CUDA_TRY(cudaStreamWaitEvent(s->st, ctx->ev_done[gk], 0));
         if (s->mode != 2)
             CUDA_TRY(cudaEventRecord(s->ev_free[s->cur], G));
         s->commit_batch();
