@@ -27,7 +27,7 @@ namespace smip_gpu {
 
 constexpr int kRecoThreads = 512;
 constexpr int kVisitChunk = 2048;
-constexpr int kSlots = (65 * 65 + kRecoThreads - 1) / kRecoThreads; // pair slots per thread (d <= 64)
+constexpr int kMaxSlots = (65 * 65 + kRecoThreads - 1) / kRecoThreads; // pair slots per thread (d <= 64)
 
 __device__ __forceinline__ int wrap_idx(int x, int y, int W, int H)
 {
@@ -132,6 +132,9 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // and the phases phi(u) sit in shared memory; the next point's row and phase
 // gathers are already in flight (cp.async, double-buffered), so the serial
 // path per point is: flag checks, two complex products, the reductions.
+// kSlots = ceil((d+1)^2 / 512) pair slots per thread, fixed at compile time so
+// that a small depth does not pay for the largest one's slot loop.
+template <int kSlots>
 __global__ void __launch_bounds__(kRecoThreads, 1) phase_chain_kernel(const RecoJob* __restrict__ jobs)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -361,14 +364,29 @@ cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int
     note_launches(1);
     const size_t smem = sizeof(float2) * 5 * nv + sizeof(int2) * kVisitChunk
                         + sizeof(unsigned int) * (((size_t)max_W * max_H + 31) / 32);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(phase_chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess)
-            return e;
+    const int slots = (nv + kRecoThreads - 1) / kRecoThreads;
+    auto launch = [&](auto kern) -> cudaError_t {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess)
+                return e;
+        }
+        kern<<<njobs, kRecoThreads, smem, st>>>(jobs_dev);
+        note_launches(1);
+        return cudaGetLastError();
+    };
+    static_assert(kMaxSlots == 9, "slot instantiations");
+    switch (slots) {
+    case 1: return launch(phase_chain_kernel<1>);
+    case 2: return launch(phase_chain_kernel<2>);
+    case 3: return launch(phase_chain_kernel<3>);
+    case 4: return launch(phase_chain_kernel<4>);
+    case 5: return launch(phase_chain_kernel<5>);
+    case 6: return launch(phase_chain_kernel<6>);
+    case 7: return launch(phase_chain_kernel<7>);
+    case 8: return launch(phase_chain_kernel<8>);
+    default: return launch(phase_chain_kernel<9>);
     }
-    phase_chain_kernel<<<njobs, kRecoThreads, smem, st>>>(jobs_dev);
-    note_launches(1);
-    return cudaGetLastError();
 }
 
 } // namespace smip_gpu
