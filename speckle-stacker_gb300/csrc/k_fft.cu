@@ -227,7 +227,8 @@ __global__ void power_reduce_kernel(double* __restrict__ P, const double* __rest
 // imaginary parts); two rows per complex FFT.  Output: unnormalised
 // correlation c[y][x] = W*H * sum ref(p) frame(p + (x,y)).
 __global__ void __launch_bounds__(256) xcorr_rows_kernel(const float2* __restrict__ Gt, float* __restrict__ corr,
-                                                          int logW, int H, int hw, const float2* __restrict__ tw_g)
+                                                          float* __restrict__ rowmax, int logW, int H, int hw,
+                                                          const float2* __restrict__ tw_g)
 {
     extern __shared__ float2 sm[];
     const int W = 1 << logW;
@@ -273,6 +274,21 @@ __global__ void __launch_bounds__(256) xcorr_rows_kernel(const float2* __restric
         const float2 v = lines[(r >> 1) * LW + pad8(x)];
         out[idx] = (r & 1) ? v.y : v.x;
     }
+    // every row's maximum (16 threads per row), so that the peak search reads
+    // the rows that can hold candidates only
+    static_assert(kRowBlock * 16 == 256, "16 threads per row");
+    const int r = threadIdx.x >> 4, sub = threadIdx.x & 15;
+    const float2* Lr = lines + (r >> 1) * LW;
+    float m = -INFINITY;
+    for (int x = sub; x < W; x += 16) {
+        const float2 v = Lr[pad8(x)];
+        m = fmaxf(m, (r & 1) ? v.y : v.x);
+    }
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1)
+        m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (sub == 0)
+        rowmax[(long long)f * H + y0 + r] = m;
 }
 
 // ----------------------------------------------------- spectrum import
@@ -360,15 +376,15 @@ cudaError_t launch_power_reduce(double* P, const double* Ppart, int nchunks, con
     return cudaGetLastError();
 }
 
-cudaError_t launch_xcorr_rows(const float2* T, float* corr, int nframes, const Geometry& g, const float2* tw,
-                              cudaStream_t st)
+cudaError_t launch_xcorr_rows(const float2* T, float* corr, float* rowmax, int nframes, const Geometry& g,
+                              const float2* tw, cudaStream_t st)
 {
     const dim3 grid(g.H / kRowBlock, nframes);
     const size_t smem = sizeof(float2) * (g.W + g.hw * (kRowBlock + 1) + (kRowBlock / 2) * pad8(g.W));
     cudaError_t e = allow_smem(xcorr_rows_kernel, smem);
     if (e != cudaSuccess)
         return e;
-    xcorr_rows_kernel<<<grid, 256, smem, st>>>(T, corr, g.logW, g.H, g.hw, tw);
+    xcorr_rows_kernel<<<grid, 256, smem, st>>>(T, corr, rowmax, g.logW, g.H, g.hw, tw);
     note_launches(1);
     return cudaGetLastError();
 }

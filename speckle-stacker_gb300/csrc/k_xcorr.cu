@@ -127,6 +127,7 @@ __device__ void exact_corr_multi(const T* __restrict__ ref, const T* __restrict_
 
 template <typename T>
 __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float* __restrict__ corr,
+                                                                     const float* __restrict__ rowmax,
                                                                      const T* __restrict__ frames, long long fstride,
                                                                      const T* __restrict__ ref, const double* ref_sq,
                                                                      int first_is_frame0, int W, int H,
@@ -148,16 +149,17 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
     }
     const int n = W * H;
     const float* c = corr + (long long)f * n;
+    const float* rm = rowmax + (long long)f * H;
     const T* fr = frames + (long long)f * fstride;
-    // ||frame||^2 and the FP32 peak.  corr rows are 16-byte aligned (n is a
-    // multiple of 256); the frame uses vector loads when its address allows.
+    // ||frame||^2 (the frame uses vector loads when its address allows) and
+    // the FP32 peak from the rows' maxima
     A sqa = 0; // exact (u64) for integer frames, FP64 for float frames
     float mx = -INFINITY;
+    for (int y = threadIdx.x; y < H; y += blockDim.x)
+        mx = fmaxf(mx, rm[y]);
     constexpr int PV = sizeof(T) == 8 ? 2 : 4;           // pixels per frame vector load
     const bool vec = (reinterpret_cast<uintptr_t>(fr) & 15) == 0;
     for (int p = threadIdx.x * 4; p < n; p += blockDim.x * 4) {
-        const float4 cv = *reinterpret_cast<const float4*>(c + p);
-        mx = fmaxf(fmaxf(mx, fmaxf(cv.x, cv.y)), fmaxf(cv.z, cv.w));
         if (vec) {
 #pragma unroll
             for (int q = 0; q < 4; q += PV) {
@@ -208,21 +210,28 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
             }
         }
     };
-    // One pass collects every position with c >= thr (the winner is chosen by
-    // exact value, then lowest index, so collection order does not matter).
+    // One pass over the rows whose maximum reaches thr collects every position
+    // with c >= thr (the winner is chosen by exact value, then lowest index, so
+    // collection order does not matter); corr rows are 16-byte aligned.
     if (threadIdx.x == 0)
         ncand = 0;
     __syncthreads();
-    for (int p = threadIdx.x * 4; p < n; p += blockDim.x * 4) {
-        const float4 cv = *reinterpret_cast<const float4*>(c + p);
-        const float e4[4] = { cv.x, cv.y, cv.z, cv.w };
+    const int lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    for (int y = threadIdx.x >> 5; y < H; y += nwarps) {
+        if (!(rm[y] >= thr))
+            continue;
+        for (int x = lane * 4; x < W; x += 128) {
+            const int p = y * W + x;
+            const float4 cv = *reinterpret_cast<const float4*>(c + p);
+            const float e4[4] = { cv.x, cv.y, cv.z, cv.w };
 #pragma unroll
-        for (int e = 0; e < 4; ++e)
-            if (e4[e] >= thr) {
-                const int slot = atomicAdd(&ncand, 1);
-                if (slot < kMaxCand)
-                    cand[slot] = p + e;
-            }
+            for (int e = 0; e < 4; ++e)
+                if (e4[e] >= thr) {
+                    const int slot = atomicAdd(&ncand, 1);
+                    if (slot < kMaxCand)
+                        cand[slot] = p + e;
+                }
+        }
     }
     __syncthreads();
     const int total_cand = ncand;
@@ -334,15 +343,15 @@ __global__ void sumsq_kernel(const T* __restrict__ fr, long long n, double* out)
         *out = s;
 }
 
-cudaError_t launch_xcorr_shift(int dtype, const float* corr, const void* frames, long long fstride, const void* ref,
-                               const double* ref_sq, int nframes, int first_is_frame0, const Geometry& g, int* shifts,
-                               cudaStream_t st)
+cudaError_t launch_xcorr_shift(int dtype, const float* corr, const float* rowmax, const void* frames, long long fstride,
+                               const void* ref, const double* ref_sq, int nframes, int first_is_frame0,
+                               const Geometry& g, int* shifts, cudaStream_t st)
 {
     switch (dtype) {
-    case 0: xcorr_shift_kernel<uint8_t><<<nframes, kShiftThreads, 0, st>>>(corr, (const uint8_t*)frames, fstride, (const uint8_t*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
-    case 1: xcorr_shift_kernel<uint16_t><<<nframes, kShiftThreads, 0, st>>>(corr, (const uint16_t*)frames, fstride, (const uint16_t*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
-    case 2: xcorr_shift_kernel<float><<<nframes, kShiftThreads, 0, st>>>(corr, (const float*)frames, fstride, (const float*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
-    default: xcorr_shift_kernel<double><<<nframes, kShiftThreads, 0, st>>>(corr, (const double*)frames, fstride, (const double*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
+    case 0: xcorr_shift_kernel<uint8_t><<<nframes, kShiftThreads, 0, st>>>(corr, rowmax, (const uint8_t*)frames, fstride, (const uint8_t*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
+    case 1: xcorr_shift_kernel<uint16_t><<<nframes, kShiftThreads, 0, st>>>(corr, rowmax, (const uint16_t*)frames, fstride, (const uint16_t*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
+    case 2: xcorr_shift_kernel<float><<<nframes, kShiftThreads, 0, st>>>(corr, rowmax, (const float*)frames, fstride, (const float*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
+    default: xcorr_shift_kernel<double><<<nframes, kShiftThreads, 0, st>>>(corr, rowmax, (const double*)frames, fstride, (const double*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
     }
     return cudaGetLastError();
 }

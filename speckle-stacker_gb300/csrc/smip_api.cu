@@ -344,6 +344,7 @@ struct smip_stack {
     dfc* Gt = nullptr;            // row-FFT output, float-float
     float2 *T = nullptr, *S = nullptr, *R = nullptr;
     float* corr = nullptr;
+    float* rowmax = nullptr;      // per frame and row: the correlation's maximum
     float2* kscratch = nullptr;   // bispectrum kernel: partial sums of split tiles
     int* ktile_cnt = nullptr;     // bispectrum kernel: parts finished per split tile
     int* shifts = nullptr;        // all frames, int2
@@ -379,7 +380,7 @@ struct smip_stack {
             cudaStreamDestroy(cst);
         dfree(spec_staging);
         if (ref) cudaFree(ref);
-        dfree(ref_sq); dfree(Gt); dfree(T); dfree(S); dfree(R); dfree(corr); dfree(shifts); dfree(err);
+        dfree(ref_sq); dfree(Gt); dfree(T); dfree(S); dfree(R); dfree(corr); dfree(rowmax); dfree(shifts); dfree(err);
         dfree(kscratch); dfree(ktile_cnt);
         dfree(Z); dfree(pfull); dfree(maxbuf);
         for (auto& e : ev_pool) {
@@ -411,6 +412,7 @@ struct smip_stack {
         CUDA_TRY(cudaMalloc(&S, sizeof(float2) * half_elems() * Bf));
         CUDA_TRY(cudaMalloc(&R, sizeof(float2) * half_elems()));
         CUDA_TRY(cudaMalloc(&corr, sizeof(float) * frame_elems() * Bf));
+        CUDA_TRY(cudaMalloc(&rowmax, sizeof(float) * g.H * Bf));
         CUDA_TRY(cudaMalloc(&ref_sq, sizeof(double)));
         CUDA_TRY(cudaMalloc(&err, sizeof(int)));
         CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
@@ -509,9 +511,9 @@ struct smip_stack {
             CUDA_TRY(launch_col_pass(0, Gt, S, R, nullptr, T, Ppart, n, fpc, first ? 1 : 0, g, ctx->twdf, ctx->tw32,
                                      q));
             CUDA_TRY(launch_power_reduce(P, Ppart, (n + fpc - 1) / fpc, g, q));
-            CUDA_TRY(launch_xcorr_rows(T, corr, n, g, ctx->tw32, q));
-            CUDA_TRY(launch_xcorr_shift(dtype, corr, staging, (long long)fe, ref, ref_sq, n, first ? 1 : 0, g,
-                                        shifts + 2 * first_index, q));
+            CUDA_TRY(launch_xcorr_rows(T, corr, rowmax, n, g, ctx->tw32, q));
+            CUDA_TRY(launch_xcorr_shift(dtype, corr, rowmax, staging, (long long)fe, ref, ref_sq, n, first ? 1 : 0,
+                                        g, shifts + 2 * first_index, q));
             CUDA_TRY(launch_saa_add(dtype, sum, staging, (long long)fe, n, first ? 1 : 0, shifts + 2 * first_index, g, q));
         }
         BispecLaunch L;

@@ -57,14 +57,15 @@ cudaError_t launch_col_pass(int mode, const dfc* Gt, float2* S, const float2* Rb
 cudaError_t launch_power_reduce(double* P, const double* Ppart, int nchunks, const Geometry& g, cudaStream_t st);
 
 // Row pass of the correlation's inverse transform: corr[f][y][x] (float).
-cudaError_t launch_xcorr_rows(const float2* T, float* corr, int nframes, const Geometry& g, const float2* tw,
-                              cudaStream_t st);
+// corr: [nframes][H][W] correlation; rowmax: [nframes][H] maximum of each row
+cudaError_t launch_xcorr_rows(const float2* T, float* corr, float* rowmax, int nframes, const Geometry& g,
+                              const float2* tw, cudaStream_t st);
 
 // Integer shift per frame: FP32 correlation peak, candidates re-scored exactly.
 // ref_sq: sum of squares of the reference frame (double, device).
-cudaError_t launch_xcorr_shift(int dtype, const float* corr, const void* frames, long long frame_stride_elems,
-                               const void* ref, const double* ref_sq, int nframes, int first_is_frame0,
-                               const Geometry& g, int* shifts, cudaStream_t st);
+cudaError_t launch_xcorr_shift(int dtype, const float* corr, const float* rowmax, const void* frames,
+                               long long frame_stride_elems, const void* ref, const double* ref_sq, int nframes,
+                               int first_is_frame0, const Geometry& g, int* shifts, cudaStream_t st);
 
 // sum += |frames| shifted back by their shifts (Array2::shifted semantics);
 // the stack's frame 0 enters with its sign (smip-cli/main.cpp:266).

@@ -43,7 +43,8 @@ constexpr size_t kOffT = kOffS + align256(kHalf * sizeof(float2));       // 1 fr
 constexpr size_t kOffR = kOffT + align256(kHalf * sizeof(float2));       // reference spectrum
 constexpr size_t kOffP = kOffR + align256(kHalf * sizeof(float2));       // power partials
 constexpr size_t kOffC = kOffP + align256(kHalf * sizeof(double));       // correlation
-constexpr size_t kOffQ = kOffC + align256((size_t)kMaxN * kMaxN * sizeof(float)); // sum of squares
+constexpr size_t kOffM = kOffC + align256((size_t)kMaxN * kMaxN * sizeof(float)); // row maxima
+constexpr size_t kOffQ = kOffM + align256((size_t)kMaxN * sizeof(float));          // sum of squares
 constexpr int kTw = 1 << (kTwLog - 1);
 constexpr size_t kOffTw = kOffQ + 256;                                   // FP32 twiddles
 constexpr size_t kOffTwDf = kOffTw + align256(kTw * sizeof(float2));     // float-float twiddles
@@ -132,6 +133,7 @@ extern "C" int smip_xcorr_displacement_noalloc(const double* ref, const double* 
     float2* R = reinterpret_cast<float2*>(base + kOffR);
     double* Pp = reinterpret_cast<double*>(base + kOffP);
     float* corr = reinterpret_cast<float*>(base + kOffC);
+    float* rowmax = reinterpret_cast<float*>(base + kOffM);
     double* refsq = reinterpret_cast<double*>(base + kOffQ);
     const float2* tw = reinterpret_cast<const float2*>(base + kOffTw);
     const dfc* twdf = reinterpret_cast<const dfc*>(base + kOffTwDf);
@@ -142,8 +144,8 @@ extern "C" int smip_xcorr_displacement_noalloc(const double* ref, const double* 
     if (e == cudaSuccess) e = launch_row_pass(SMIP_F64, frame, n, 1, g, Gt + half, twdf, st);
     if (e == cudaSuccess) e = launch_col_pass(1, Gt, S, R, R, T, Pp, 1, 16, 0, g, twdf, tw, st);
     if (e == cudaSuccess) e = launch_col_pass(0, Gt + half, S, R, nullptr, T, Pp, 1, 16, 0, g, twdf, tw, st);
-    if (e == cudaSuccess) e = launch_xcorr_rows(T, corr, 1, g, tw, st);
-    if (e == cudaSuccess) e = launch_xcorr_shift(SMIP_F64, corr, frame, n, ref, refsq, 1, 0, g, shift, st);
+    if (e == cudaSuccess) e = launch_xcorr_rows(T, corr, rowmax, 1, g, tw, st);
+    if (e == cudaSuccess) e = launch_xcorr_shift(SMIP_F64, corr, rowmax, frame, n, ref, refsq, 1, 0, g, shift, st);
     if (e != cudaSuccess)
         return fail(SMIP_E_CUDA, cudaGetErrorString(e));
     return SMIP_OK;

@@ -80,6 +80,19 @@ def test_extended256_sample(smip, oracle):
     check_against(out, exp, fp64_bispec=exp["bispec"])
 
 
+def test_extended512_sample(smip, oracle):
+    """4 frames of the 512x512 u16 workload (200 blobs + disk, D/r0 = 25),
+    -b 48 -p 200, against the FP64 oracle: the largest frame and the depth-48
+    bispectrum tile."""
+    from smip_gb300 import synthetic as S
+
+    spec = S.config_spec("extended512", nframes=4)
+    frames = S.make_stack(spec)
+    exp = oracle.run_stack(frames, spec.bdepth, spec.reco_radius, fp64=True, nthreads=16)
+    out = run_gpu(smip, frames, spec.bdepth, spec.reco_radius)
+    check_against(out, exp, fp64_bispec=exp["bispec"])
+
+
 def test_default_depth_pipeline(smip, oracle):
     """smip-cli's default depth -b 20 (not a multiple of 8) through the whole
     pipeline, 128x128 u8 binary star, against the FP64 oracle."""
