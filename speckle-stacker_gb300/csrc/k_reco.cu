@@ -6,28 +6,31 @@
 //     phi(u) phi(v) conj(B(u,v) / |B(u,v)|)    over u + v = w,
 // u and v flagged, |B| > DBL_EPSILON, v inside the bispectrum's v range.
 // Each point may use phases set earlier in the same ring, so the walk is a
-// strict serial chain; the parallelism is inside a point: the (d+1)^2
-// candidate pairs are spread over the 512 threads of the block.
-//
-// Latency structure of one point: the bispectrum gathers depend only on w, not
-// on the chain, so the gathers of the NEXT point are issued before the
-// current point is reduced (software pipelining); the visit list is staged in
-// shared memory; phases of the small v disc live in shared memory.
+// serial chain.  Most of a point's pairs, though, read phases that were final
+// long before: a pair is "recent" only when u or v was visited within the
+// kRecoLag visits before w (the arc of the ring just behind w).  The walk is
+// therefore split (one CTA per job):
+//   - warps 1..15 form, for visit q, the sum over its non-recent pairs as soon
+//     as the walk has passed q - kRecoLag, eight pair slots per lane at a time
+//     so that the plan, flag and phase gathers overlap;
+//   - warp 0 runs the visits in order and adds only the recent pairs (a list
+//     of at most kRecentMax per visit, prefetched with the plan phasors) to
+//     that share, then sets the point's phase and flag.
+// Which pairs are recent depends only on the visit list (per point: its visit
+// indices), so it is computed in parallel before the walk.
 //
 // Precision: per-pair products in FP32 from an FP32 mirror of the phase map
-// (~1e-7 rad per pair); the phasor sums are compensated (float-float, ~48-bit)
-// through the thread, warp and block reductions, because at low-consistency
-// points the mean phasor is a large cancellation; the mean, |mean|
-// (consistency) and the stored phase are FP64.  B is read through a device
-// replica of Bispectrum::get_element's index arithmetic, aliasing included.
-// One CTA per job; many jobs (stacks) run in one launch.
+// (~1e-7 rad per pair); the non-recent share is summed in FP32 per lane and in
+// float-float over the lanes, and the recent pairs are added to it in
+// float-float, because at low-consistency points the mean phasor is a large
+// cancellation; the mean, |mean| (consistency) and the stored phase are FP64.
+// B is read through a device replica of Bispectrum::get_element's index
+// arithmetic, aliasing included.
 #include "smip_dev.cuh"
 
 namespace smip_gpu {
 
 constexpr int kRecoThreads = 512;
-constexpr int kVisitChunk = 2048;
-constexpr int kMaxSlots = (65 * 65 + kRecoThreads - 1) / kRecoThreads; // pair slots per thread (d <= 64)
 
 __device__ __forceinline__ int wrap_idx(int x, int y, int W, int H)
 {
@@ -120,43 +123,145 @@ __global__ void __launch_bounds__(256) reco_plan_kernel(const RecoJob* __restric
     }
 }
 
-// ---------------------------------------------------------------- chain
-__device__ __forceinline__ void cp_async8(void* smem_dst, const void* gmem_src)
+// ------------------------------------------------------ pipelined walk
+// A visit's pairs split by when their phases became final.  A pair (u, v)
+// of visit q is "recent" when u or v was visited within the kRecoLag visits
+// before q (visit lists per point: pvis); every other pair only reads phases
+// and flags that no visit in [q - kRecoLag, q) can change, so its share of
+// the sum can be formed as soon as the walk has passed q - kRecoLag.  The
+// serial part of a visit is then the few recent pairs (the arc of the current
+// ring just behind w) instead of all (d+1)^2.
+__device__ __forceinline__ bool visited_in_lag(int4 pv, int q)
 {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(smem_dst)), "l"(gmem_src) : "memory");
+    if (pv.w > 3) // more visits than recorded: treat as recent
+        return true;
+    const int lo = q - kRecoLag;
+    return (pv.x >= 0 && pv.x >= lo && pv.x < q) || (pv.y >= 0 && pv.y >= lo && pv.y < q)
+           || (pv.z >= 0 && pv.z >= lo && pv.z < q);
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// One CTA per job walks the spiral.  For the point being reduced the plan row
-// and the phases phi(u) sit in shared memory; the next point's row and phase
-// gathers are already in flight (cp.async, double-buffered), so the serial
-// path per point is: flag checks, two complex products, the reductions.
-// kSlots = ceil((d+1)^2 / 512) pair slots per thread, fixed at compile time so
-// that a small depth does not pay for the largest one's slot loop.
-template <int kSlots>
-__global__ void __launch_bounds__(kRecoThreads, 1) phase_chain_kernel(const RecoJob* __restrict__ jobs)
+__global__ void __launch_bounds__(256) reco_recent_kernel(const RecoJob* __restrict__ jobs)
+{
+    const RecoJob J = jobs[blockIdx.y];
+    const int W = J.W, H = J.H, De = J.De;
+    const int nside = De + 1, nv = nside * nside, nwords = (nv + 31) / 32;
+    const int pmin0 = -(W >> 1), pmin1 = -(H >> 1);
+    const int pmax0 = -W / 2 + W - 1, pmax1 = -H / 2 + H - 1;
+    const long long total = (long long)J.nvisits * nwords;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int q = (int)(e / nwords), wd = (int)(e - (long long)q * nwords);
+        const int2 w = J.visits[q];
+        unsigned bits = 0u;
+        if (!(w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1)) {
+            for (int b = 0; b < 32; ++b) {
+                const int t = wd * 32 + b;
+                if (t >= nv)
+                    break;
+                const int vx = -De / 2 + t % nside, vy = -De / 2 + t / nside;
+                const int ux = w.x - vx, uy = w.y - vy;
+                if (ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1)
+                    continue;
+                if (visited_in_lag(J.pvis[wrap_idx(ux, uy, W, H)], q) || visited_in_lag(J.pvis[wrap_idx(vx, vy, W, H)], q))
+                    bits |= 1u << b;
+            }
+        }
+        J.rbits[e] = bits;
+    }
+}
+
+// One warp per visit: the recent pair slots in increasing order, or -1 when
+// there are more than kRecentMax (the serial warp then takes every pair).
+__global__ void __launch_bounds__(256) reco_rlist_kernel(const RecoJob* __restrict__ jobs)
+{
+    const RecoJob J = jobs[blockIdx.y];
+    const int nv = (J.De + 1) * (J.De + 1), nwords = (nv + 31) / 32;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int q = gw; q < J.nvisits; q += nw) {
+        const unsigned* rb = J.rbits + (long long)q * nwords;
+        int base = 0;
+        for (int w0 = 0; w0 < nwords; w0 += 32) {
+            const unsigned bits = w0 + lane < nwords ? rb[w0 + lane] : 0u;
+            const int c = __popc(bits);
+            int incl = c; // inclusive prefix over the lanes
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o)
+                    incl += y;
+            }
+            int pos = base + incl - c;
+            unsigned b = bits;
+            while (b) {
+                const int k = __ffs(b) - 1;
+                b &= b - 1;
+                if (pos < kRecentMax)
+                    J.rlist[(long long)q * kRecentMax + pos] = (unsigned short)((w0 + lane) * 32 + k);
+                ++pos;
+            }
+            base += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (lane == 0)
+            J.rcount[q] = base > kRecentMax ? -1 : base;
+    }
+}
+
+// The walk, one CTA per job.  Warp 0 runs the visits in order: for visit q it
+// waits for the share of the non-recent pairs, adds the recent pairs (or all
+// pairs when the list overflowed), forms the phase and advances `progress`.
+// Warps 1..15 form the non-recent shares of visits q = warp-1 (mod 15), each
+// once progress >= q - kRecoLag, into a ring of kRing slots.  Every wait is
+// bounded; on a timeout the walk stops and the error is recorded.
+constexpr int kRing = 64;
+constexpr int kPhaseCache = 2048;
+
+// CTA-scope acquire load / release store on shared memory: they order the
+// accesses after (before) them without waiting for this thread's other
+// outstanding loads, as a full fence would.
+__device__ __forceinline__ int ld_acquire_cta(const int* p)
+{
+    int v;
+    asm volatile("ld.acquire.cta.shared.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_cta(int* p, int v)
+{
+    asm volatile("st.release.cta.shared.b32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
+}
+static_assert(kRing > kRecoLag + 1, "ring slots outlive the lag");
+constexpr unsigned long long kRecoWaitNs = 2000000000ull;
+
+__global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJob* __restrict__ jobs)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ float red[3][32];
-    __shared__ int red_n[32];
-    __shared__ int last_pw;
-    __shared__ float2 last_ph;
+    __shared__ float4 ring_s[kRing];
+    __shared__ int ring_n[kRing];
+    __shared__ int ring_tag[kRing];
+    __shared__ int progress;
+    __shared__ int abort_walk;
+    __shared__ int pc_key[kPhaseCache];   // serial warp: phases it set, by point
+    __shared__ float2 pc_val[kPhaseCache];
     const RecoJob J = jobs[blockIdx.x];
     const int W = J.W, H = J.H, De = J.De;
     const int nbits = W * H;
-    const int nside = De + 1, nv = nside * nside;
-    float2* rowbuf = reinterpret_cast<float2*>(smraw);          // [2][nv] plan rows
-    float2* phubuf = rowbuf + 2 * nv;                            // [2][nv] phi(u) gathers
-    float2* vtab = phubuf + 2 * nv;                              // [nv] phases of the v disc
-    int2* vis = reinterpret_cast<int2*>(vtab + nv);              // [kVisitChunk]
-    unsigned int* flagbits = reinterpret_cast<unsigned int*>(vis + kVisitChunk); // [W*H bits]
+    const int nside = De + 1, nv = nside * nside, nwords = (nv + 31) / 32;
+    float2* vtab = reinterpret_cast<float2*>(smraw);                        // [nv] phases of the v disc
+    int2* slot_v = reinterpret_cast<int2*>(vtab + nv);                      // [nv] (vx | vy << 16, map index of v)
+    unsigned int* flagbits = reinterpret_cast<unsigned int*>(slot_v + nv);  // [W*H bits]
     for (int i = threadIdx.x; i < (nbits + 31) / 32; i += blockDim.x)
         flagbits[i] = 0u;
-    for (int i = threadIdx.x; i < nv; i += blockDim.x)
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
         vtab[i] = make_float2(0.f, 0.f);
-    if (threadIdx.x == 0)
-        last_pw = -1;
+        const int vx = -De / 2 + i % nside, vy = -De / 2 + i / nside;
+        slot_v[i] = make_int2((int)(((unsigned)vx & 0xffffu) | ((unsigned)vy << 16)), wrap_idx(vx, vy, W, H));
+    }
+    for (int i = threadIdx.x; i < kRing; i += blockDim.x)
+        ring_tag[i] = -1;
+    if (threadIdx.x == 0) {
+        progress = 0;
+        abort_walk = 0;
+    }
     __syncthreads();
     if (threadIdx.x < 5) { // seeds (phasereco.h:42-54); all inside the v disc
         const int sx[5] = { 0, 1, 0, -1, 0 }, sy[5] = { 0, 0, 1, 0, -1 };
@@ -168,91 +273,159 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_chain_kernel(const Reco
         vtab[(sy[threadIdx.x] + De / 2) * nside + sx[threadIdx.x] + De / 2] = make_float2(1.f, im);
         atomicOr(&flagbits[p >> 5], 1u << (p & 31));
     }
+    __syncthreads();
     const int pmin0 = -(W >> 1), pmin1 = -(H >> 1);
     const int pmax0 = -W / 2 + W - 1, pmax1 = -H / 2 + H - 1;
     const int szW = (W / 2) * 2 + 1, szH = (H / 2) * 2 + 1;
     const int umn0 = -(szW / 2), umx0 = szW - szW / 2 - 1, umn1 = -(szH / 2), umx1 = szH - szH / 2 - 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    volatile int* vabort = &abort_walk;
 
-    // This thread's pair slots t = threadIdx.x + k * kRecoThreads and their v
-    // (and v's map index), computed once for the whole walk.
-    int svx[kSlots], svy[kSlots], spv[kSlots];
-#pragma unroll
-    for (int k = 0; k < kSlots; ++k) {
-        const int t = threadIdx.x + k * kRecoThreads;
-        svx[k] = -De / 2 + t % nside;
-        svy[k] = -De / 2 + t / nside;
-        spv[k] = t < nv ? wrap_idx(svx[k], svy[k], W, H) : 0;
-    }
-
-    // each thread copies its own slots and later reads only what it copied
-    auto prefetch = [&](int q, int2 w, int buf) {
-        const float2* row = J.plan + (long long)q * nv;
-#pragma unroll
-        for (int k = 0; k < kSlots; ++k) {
-            const int t = threadIdx.x + k * kRecoThreads;
-            if (t < nv) {
-                cp_async8(&rowbuf[buf * nv + t], &row[t]);
-                const int ux = w.x - svx[k], uy = w.y - svy[k];
-                if (!(ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1))
-                    cp_async8(&phubuf[buf * nv + t], &J.phf[wrap_idx(ux, uy, W, H)]);
+    auto flag = [&](int p) { return ((flagbits[p >> 5] >> (p & 31)) & 1u) != 0u; };
+    // bounded wait on a shared-memory condition; false on a timeout (then the walk stops)
+    auto wait_until = [&](auto cond) {
+        if (cond())
+            return true;
+        const unsigned long long t0 = globaltimer_ns();
+        for (;;) {
+            for (int i = 0; i < 64; ++i)
+                if (cond())
+                    return true;
+            if (*vabort)
+                return false;
+            if (globaltimer_ns() - t0 > kRecoWaitNs) {
+                record_error(J.err, SMIP_DEV_ERR_TIMEOUT);
+                *vabort = 1;
+                return false;
             }
         }
-        cp_async_commit();
     };
 
-    __syncthreads();
-    int2 wcur = J.visits[0];
-    prefetch(0, wcur, 0);
-    for (int q0 = 0; q0 < J.nvisits; q0 += kVisitChunk) {
-        const int nq = min(kVisitChunk, J.nvisits - q0);
-        __syncthreads();
-        for (int i = threadIdx.x; i < nq; i += blockDim.x)
-            vis[i] = J.visits[q0 + i];
-        __syncthreads();
-        for (int qi = 0; qi < nq; ++qi) {
-            const int q = q0 + qi;
-            const int buf = q & 1;
-            // this point's copies (issued one point ago) land; only then is the
-            // other buffer free for the next point's copies
-            cp_async_wait_all();
-            int2 wn = make_int2(0, 0);
-            if (q + 1 < J.nvisits) {
-                wn = qi + 1 < nq ? vis[qi + 1] : J.visits[q + 1];
-                prefetch(q + 1, wn, buf ^ 1);
+    // Pairs of visit q, eight slots per lane at a time, so that the plan,
+    // flag and phase gathers overlap; skip_recent leaves the recent pairs
+    // out (the serial warp takes them); phase reads the phase map.
+    auto sum_pairs = [&](int q, int2 w, bool skip_recent, auto phase, float& sr, float& si, int& cnt) {
+        constexpr int kB = 8;
+        const unsigned* rb = J.rbits + (long long)q * nwords;
+        const float2* prow = J.plan + (long long)q * nv;
+        for (int i0 = 0; i0 < nwords; i0 += kB) {
+            float2 bh[kB], ph[kB];
+            int tt[kB];
+            bool use[kB];
+#pragma unroll
+            for (int k = 0; k < kB; ++k) {
+                const int t = lane + 32 * (i0 + k);
+                tt[k] = t;
+                use[k] = i0 + k < nwords && t < nv;
+                // slot t's bit is bit `lane` of word i0 + k
+                if (skip_recent)
+                    use[k] = use[k] && !((rb[i0 + k] >> lane) & 1u);
+                bh[k] = use[k] ? prow[t] : make_float2(0.f, 0.f);
+                if (use[k]) { // flags and the phase gather do not wait for the plan
+                    const int2 sv = slot_v[t];
+                    const int vx = (int)(short)(sv.x & 0xffff), vy = sv.x >> 16;
+                    const int ux = w.x - vx, uy = w.y - vy;
+                    const bool inu = !(ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1);
+                    const int pu = inu ? wrap_idx(ux, uy, W, H) : 0, pv = sv.y;
+                    use[k] = inu && flag(pu) && flag(pv);
+                    ph[k] = use[k] ? phase(pu) : make_float2(0.f, 0.f);
+                }
             }
-            const int2 w = wcur;
+#pragma unroll
+            for (int k = 0; k < kB; ++k) {
+                if (!use[k] || (bh[k].x == 0.f && bh[k].y == 0.f)) // the plan's zero: never contributes
+                    continue;
+                if (isnan(bh[k].x)) {
+                    record_error(J.err, SMIP_DEV_ERR_OUT_OF_RANGE);
+                    continue;
+                }
+                const float2 p = cmul(cmul(ph[k], vtab[tt[k]]), make_float2(bh[k].x, -bh[k].y));
+                const float r = rsqrtf(p.x * p.x + p.y * p.y);
+                sr += p.x * r;
+                si += p.y * r;
+                ++cnt;
+            }
+        }
+    };
+
+    if (warp == 0) {
+        // ------------------------------------------------ serial warp
+        // Visit data that does not depend on the walk is loaded ahead: the
+        // visit, its recent-pair count and slots two visits ahead, their plan
+        // phasors one visit ahead.  Phases the walk just set come from a
+        // shared-memory cache keyed by point (a miss reads the phase map).
+        for (int i = lane; i < kPhaseCache; i += 32)
+            pc_key[i] = -1;
+        __syncwarp();
+        struct Ahead {
+            int2 w;
+            int rc, ta, tb;
+            float2 ba, bb;
+        };
+        auto load_meta = [&](int q, Ahead& a) {
+            if (q >= J.nvisits)
+                return;
+            a.w = J.visits[q];
+            a.rc = J.rcount[q];
+            const unsigned short* rl = J.rlist + (long long)q * kRecentMax;
+            a.ta = lane < a.rc ? (int)rl[lane] : -1;
+            a.tb = lane + 32 < a.rc ? (int)rl[lane + 32] : -1;
+        };
+        auto load_plan = [&](int q, Ahead& a) {
+            if (q >= J.nvisits)
+                return;
+            const float2* prow = J.plan + (long long)q * nv;
+            a.ba = a.ta >= 0 ? prow[a.ta] : make_float2(0.f, 0.f);
+            a.bb = a.tb >= 0 ? prow[a.tb] : make_float2(0.f, 0.f);
+        };
+        Ahead c0 {}, c1 {}, c2 {};
+        load_meta(0, c0);
+        load_plan(0, c0);
+        load_meta(1, c1);
+        auto phase_of = [&](int p) {
+            const int h = p & (kPhaseCache - 1);
+            return pc_key[h] == p ? pc_val[h] : J.phf[p];
+        };
+        auto term_s = [&](int t, float2 bh, int2 w, float& sr, float& si, int& cnt) {
+            if (bh.x == 0.f && bh.y == 0.f)
+                return;
+            const int2 sv = slot_v[t];
+            const int vx = (int)(short)(sv.x & 0xffff), vy = sv.x >> 16;
+            const int pu = wrap_idx(w.x - vx, w.y - vy, W, H), pv = sv.y;
+            if (!flag(pu) || !flag(pv))
+                return;
+            if (isnan(bh.x)) {
+                record_error(J.err, SMIP_DEV_ERR_OUT_OF_RANGE);
+                return;
+            }
+            const float2 ph = cmul(cmul(phase_of(pu), vtab[t]), make_float2(bh.x, -bh.y));
+            const float r = rsqrtf(ph.x * ph.x + ph.y * ph.y);
+            sr += ph.x * r;
+            si += ph.y * r;
+            ++cnt;
+        };
+        for (int q = 0; q < J.nvisits; ++q) {
+            load_plan(q + 1, c1); // its slots were loaded one visit ago
+            load_meta(q + 2, c2);
+            const int2 w = c0.w;
             bool run = !(w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1);
             const int pw = run ? wrap_idx(w.x, w.y, W, H) : 0;
-            run = run && !(flagbits[pw >> 5] & (1u << (pw & 31)));
+            run = run && !flag(pw);
             run = run && (abs(w.x) + abs(w.y) > 1);                                   // phasereco.h:84
             run = run && !(w.x < umn0 || w.x > umx0 || w.y < umn1 || w.y > umx1);
             if (run) {
-                const int lpw = last_pw;
-                const float2 lph = last_ph;
+                const int slot = q % kRing;
+                if (!__all_sync(0xffffffffu, wait_until([&] { return ld_acquire_cta(&ring_tag[slot]) == q; }) ? 1 : 0))
+                    break;
                 float sr = 0.f, si = 0.f;
                 int cnt = 0;
-#pragma unroll
-                for (int k = 0; k < kSlots; ++k) {
-                    const int t = threadIdx.x + k * kRecoThreads;
-                    if (t >= nv)
-                        continue;
-                    const float2 bh = rowbuf[buf * nv + t];
-                    if (bh.x == 0.f && bh.y == 0.f)
-                        continue;
-                    const int pu = wrap_idx(w.x - svx[k], w.y - svy[k], W, H), pv = spv[k];
-                    if (!(flagbits[pu >> 5] & (1u << (pu & 31))) || !(flagbits[pv >> 5] & (1u << (pv & 31))))
-                        continue;
-                    if (isnan(bh.x)) {
-                        record_error(J.err, SMIP_DEV_ERR_OUT_OF_RANGE);
-                        continue;
-                    }
-                    const float2 phu = pu == lpw ? lph : phubuf[buf * nv + t];
-                    const float2 ph = cmul(cmul(phu, vtab[t]), make_float2(bh.x, -bh.y));
-                    const float r = rsqrtf(ph.x * ph.x + ph.y * ph.y);
-                    sr += ph.x * r;
-                    si += ph.y * r;
-                    ++cnt;
+                if (c0.rc >= 0) {
+                    if (c0.ta >= 0)
+                        term_s(c0.ta, c0.ba, w, sr, si, cnt);
+                    if (c0.tb >= 0)
+                        term_s(c0.tb, c0.bb, w, sr, si, cnt);
+                } else {
+                    sum_pairs(q, w, false, phase_of, sr, si, cnt);
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
@@ -261,26 +434,13 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_chain_kernel(const Reco
                     cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
                 }
                 if (lane == 0) {
-                    red[0][warp] = sr;
-                    red[1][warp] = si;
-                    red_n[warp] = cnt;
-                }
-                __syncthreads();
-                if (warp == 0) {
-                    // float-float across warps: the mean phasor can be a large cancellation
-                    constexpr int nw = kRecoThreads / 32;
-                    float rh = lane < nw ? red[0][lane] : 0.f, rl = 0.f;
-                    float ih = lane < nw ? red[1][lane] : 0.f, il = 0.f;
-                    cnt = lane < nw ? red_n[lane] : 0;
-#pragma unroll
-                    for (int o = nw / 2; o > 0; o >>= 1) {
-                        const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
-                        const float c = __shfl_xor_sync(0xffffffffu, ih, o), e = __shfl_xor_sync(0xffffffffu, il, o);
-                        ff_add(rh, rl, a, b);
-                        ff_add(ih, il, c, e);
-                        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-                    }
-                    if (lane == 0 && cnt > 0) {
+                    // float-float: the non-recent share plus the recent one
+                    const float4 o4 = ring_s[slot];
+                    float rh = o4.x, rl = o4.y, ih = o4.z, il = o4.w;
+                    ff_add(rh, rl, sr, 0.f);
+                    ff_add(ih, il, si, 0.f);
+                    cnt += ring_n[slot];
+                    if (cnt > 0) {
                         // FP32 phase for the chain; FP64 values are formed after the walk
                         const float s2 = rh * rh + ih * ih;
                         const float lim = 2.220446049250313e-16f * (float)cnt;
@@ -294,17 +454,52 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_chain_kernel(const Reco
                         J.cnt[pw] = cnt;
                         if (abs(w.x) <= De / 2 && abs(w.y) <= De / 2)
                             vtab[(w.y + De / 2) * nside + w.x + De / 2] = pf;
+                        pc_val[pw & (kPhaseCache - 1)] = pf;
+                        pc_key[pw & (kPhaseCache - 1)] = pw;
                         flagbits[pw >> 5] |= 1u << (pw & 31);
-                        last_pw = pw;
-                        last_ph = pf;
                     }
                 }
-                __syncthreads();
+                __syncwarp();
             }
-            wcur = wn;
+            // publish progress every 8 visits: one fence (which waits for the
+            // phase-map stores) per 8 visits; the lag leaves the slack
+            if (((q & 7) == 7 || q + 1 == J.nvisits) && lane == 0)
+                st_release_cta(&progress, q + 1);
+            __syncwarp();
+            c0 = c1;
+            c1 = c2;
+        }
+    } else {
+        // ------------------------------------------- non-recent shares
+        for (int q = warp - 1; q < J.nvisits; q += kRecoThreads / 32 - 1) {
+            if (!__all_sync(0xffffffffu, wait_until([&] { return ld_acquire_cta(&progress) >= q - kRecoLag; }) ? 1 : 0))
+                break;
+            const int2 w = J.visits[q];
+            const int rc = J.rcount[q];
+            float sr = 0.f, si = 0.f;
+            int cnt = 0;
+            const bool inmap = !(w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1);
+            if (rc >= 0 && inmap)
+                sum_pairs(q, w, true, [&](int pu) { return J.phf[pu]; }, sr, si, cnt);
+            // float-float over the lanes, lane 0's order
+            float rh = sr, rl = 0.f, ih = si, il = 0.f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
+                const float c = __shfl_xor_sync(0xffffffffu, ih, o), e = __shfl_xor_sync(0xffffffffu, il, o);
+                ff_add(rh, rl, a, b);
+                ff_add(ih, il, c, e);
+                cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+            }
+            if (lane == 0) {
+                const int slot = q % kRing;
+                ring_s[slot] = make_float4(rh, rl, ih, il);
+                ring_n[slot] = cnt;
+                st_release_cta(&ring_tag[slot], q);
+            }
+            __syncwarp();
         }
     }
-    cp_async_wait_all();
     __syncthreads();
     // FP64 mean, consistency and phase of every point (phasereco.h:110-122),
     // and the flag map
@@ -362,31 +557,18 @@ cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int
     const int nv = (max_De + 1) * (max_De + 1);
     reco_plan_kernel<<<dim3(1024, njobs), 256, 0, st>>>(jobs_dev);
     note_launches(1);
-    const size_t smem = sizeof(float2) * 5 * nv + sizeof(int2) * kVisitChunk
-                        + sizeof(unsigned int) * (((size_t)max_W * max_H + 31) / 32);
-    const int slots = (nv + kRecoThreads - 1) / kRecoThreads;
-    auto launch = [&](auto kern) -> cudaError_t {
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess)
-                return e;
-        }
-        kern<<<njobs, kRecoThreads, smem, st>>>(jobs_dev);
-        note_launches(1);
-        return cudaGetLastError();
-    };
-    static_assert(kMaxSlots == 9, "slot instantiations");
-    switch (slots) {
-    case 1: return launch(phase_chain_kernel<1>);
-    case 2: return launch(phase_chain_kernel<2>);
-    case 3: return launch(phase_chain_kernel<3>);
-    case 4: return launch(phase_chain_kernel<4>);
-    case 5: return launch(phase_chain_kernel<5>);
-    case 6: return launch(phase_chain_kernel<6>);
-    case 7: return launch(phase_chain_kernel<7>);
-    case 8: return launch(phase_chain_kernel<8>);
-    default: return launch(phase_chain_kernel<9>);
-    }
+    reco_recent_kernel<<<dim3(1024, njobs), 256, 0, st>>>(jobs_dev);
+    note_launches(1);
+    reco_rlist_kernel<<<dim3(256, njobs), 256, 0, st>>>(jobs_dev);
+    note_launches(1);
+    const size_t smem = (sizeof(float2) + sizeof(int2)) * nv + sizeof(unsigned int) * (((size_t)max_W * max_H + 31) / 32);
+    // the kernel's static shared memory (ring, phase cache) counts against the same 48 KB default
+    cudaError_t e = cudaFuncSetAttribute(phase_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess)
+        return e;
+    phase_pipe_kernel<<<njobs, kRecoThreads, smem, st>>>(jobs_dev);
+    note_launches(1);
+    return cudaGetLastError();
 }
 
 } // namespace smip_gpu

@@ -208,6 +208,10 @@ struct Reco {
     Geometry g {};
     double R = -1.0;
     int2* visits = nullptr;
+    int4* pvis = nullptr;         // per point: first three visit indices, visit count
+    unsigned* rbits = nullptr;    // per visit: recent pair slots (bitmask)
+    int* rcount = nullptr;
+    unsigned short* rlist = nullptr;
     int nvisits = 0;
     double2* phases = nullptr;
     float2* phf = nullptr;
@@ -220,6 +224,10 @@ struct Reco {
     ~Reco()
     {
         dfree(visits);
+        dfree(pvis);
+        dfree(rbits);
+        dfree(rcount);
+        dfree(rlist);
         dfree(phases);
         dfree(phf);
         dfree(sums);
@@ -246,11 +254,34 @@ struct Reco {
             CUDA_TRY(cudaStreamSynchronize(st));
             dfree(visits);
             dfree(plan);
+            dfree(pvis);
+            dfree(rbits);
+            dfree(rcount);
+            dfree(rlist);
             CUDA_TRY(cudaMalloc(&visits, sizeof(int2) * v.size()));
             CUDA_TRY(cudaMemcpyAsync(visits, v.data(), sizeof(int2) * v.size(), cudaMemcpyHostToDevice, st));
             nvisits = (int)v.size();
             const size_t nv = (size_t)(g.De + 1) * (g.De + 1);
             CUDA_TRY(cudaMalloc(&plan, sizeof(float2) * nv * v.size()));
+            // each point's visits (the walk's order; a point may be visited again)
+            std::vector<int4> pv(np, make_int4(-1, -1, -1, 0));
+            const int pmin0 = -(g.W >> 1), pmin1 = -(g.H >> 1), pmax0 = g.W - 1 + pmin0, pmax1 = g.H - 1 + pmin1;
+            for (size_t q = 0; q < v.size(); ++q) {
+                const int2 w = v[q];
+                if (w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1)
+                    continue;
+                int4& e = pv[(size_t)(w.x < 0 ? w.x + g.W : w.x) + (size_t)(w.y < 0 ? w.y + g.H : w.y) * g.W];
+                if (e.w == 0) e.x = (int)q;
+                else if (e.w == 1) e.y = (int)q;
+                else if (e.w == 2) e.z = (int)q;
+                ++e.w;
+            }
+            CUDA_TRY(cudaMalloc(&pvis, sizeof(int4) * np));
+            CUDA_TRY(cudaMemcpyAsync(pvis, pv.data(), sizeof(int4) * np, cudaMemcpyHostToDevice, st));
+            const size_t nwords = (nv + 31) / 32;
+            CUDA_TRY(cudaMalloc(&rbits, sizeof(unsigned) * nwords * v.size()));
+            CUDA_TRY(cudaMalloc(&rcount, sizeof(int) * v.size()));
+            CUDA_TRY(cudaMalloc(&rlist, sizeof(unsigned short) * kRecentMax * v.size()));
             R = radius;
         }
         CUDA_TRY(cudaMemsetAsync(phases, 0, sizeof(double2) * np, st));
@@ -271,6 +302,10 @@ struct Reco {
         j.cons = cons;
         j.flags = flags;
         j.err = err;
+        j.pvis = pvis;
+        j.rbits = rbits;
+        j.rcount = rcount;
+        j.rlist = rlist;
         CUDA_TRY(cudaMemcpyAsync(job, &j, sizeof(RecoJob), cudaMemcpyHostToDevice, st));
         CUDA_TRY(launch_phase_reco(job, 1, g.W, g.H, g.De, st));
         return SMIP_OK;

@@ -110,7 +110,17 @@ struct RecoJob {
     double* cons;        // W*H
     unsigned char* flags;
     int* err;
+    // pipelined walk: per point its first three visit indices and its visit
+    // count (-1 padded); per visit the pairs whose u or v was visited within
+    // the last kRecoLag visits (bitmask over the (De+1)^2 pair slots), and
+    // their slots as a list (count -1: more than kRecentMax)
+    const int4* pvis;
+    unsigned* rbits;
+    int* rcount;
+    unsigned short* rlist;
 };
+constexpr int kRecoLag = 32;     // visits between a point's phase and the parallel stage's use of it
+constexpr int kRecentMax = 64;   // recent pairs per visit the serial warp takes from a list
 cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int max_H, int max_De, cudaStream_t st);
 // get_element index replica over a list of (ux, uy, vx, vy) tuples
 cudaError_t launch_offset_probe(const Geometry& g, const int* idx, long long n, long long* off, int* conj,
