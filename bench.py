@@ -221,7 +221,7 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-BATCHED_DESC = ("64 independent stacks queued at once: frame size from {64,128,256}, frames uniform in 50-1000, "
+BATCHED_DESC = ("64 independent stacks queued at once, each pushed whole: frame size from {64,128,256}, frames uniform in 50-1000, "
                 "binary u8 / extended u16 objects 50/50, depth 16/24/32 by size, reco radius 2 x depth")
 SERVED_DESC = ("Poisson arrivals at 20 jobs/s, 40 jobs, frame size from {64,128,256}, 100-2000 frames per job "
                "delivered in 32-frame chunks, admission by bispectrum bytes under a 120 GB budget")
@@ -232,7 +232,8 @@ def make_serving_jobs(procs):
     their frame banks are generated here, before any CUDA call."""
     from smip_gb300 import serve
 
-    batched = serve.make_jobs(64, counts=(50, 1000), rate=None, seed=3000, bank_frames=256, procs=procs)
+    # a queued stack is complete: one push per stack (the served workload below streams 32-frame chunks)
+    batched = serve.make_jobs(64, counts=(50, 1000), rate=None, seed=3000, bank_frames=256, procs=procs, chunk=1000)
     served = serve.make_jobs(40, counts=(100, 2000), rate=20.0, seed=4000, bank_frames=256, procs=procs)
     return batched, served
 
