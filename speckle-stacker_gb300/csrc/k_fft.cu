@@ -316,34 +316,42 @@ static int grid_for(long long n, int block)
     return (int)(g > 4096 ? 4096 : (g < 1 ? 1 : g));
 }
 
-template <typename K> static cudaError_t allow_smem(K kern, size_t smem)
+// The kernels' dynamic shared memory limit is set to their largest size over
+// every supported frame size (2^kMaxLog per axis), not to this launch's: the
+// attribute is per function, so concurrent launches of different shapes from
+// several host threads would otherwise lower it under each other's launches.
+template <typename K> static cudaError_t allow_smem(K kern, size_t max_smem)
 {
-    if (smem <= 48 * 1024)
-        return cudaSuccess;
-    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem);
 }
+static size_t row_pass_smem(int W) { return sizeof(dfc) * (W + (kRowBlock / 2) * (pad8(W) + 1)); }
+static size_t col_pass_smem(int H)
+{
+    return sizeof(dfc) * (H + kColLines * pad8(H)) + sizeof(float2) * (H + H + kColLines * pad8(H)) + sizeof(double) * H;
+}
+static size_t xcorr_rows_smem(int W) { return sizeof(float2) * (W + (W / 2 + 1) * (kRowBlock + 1) + (kRowBlock / 2) * pad8(W)); }
 
 cudaError_t launch_row_pass(int dtype, const void* frames, long long fstride, int nframes, const Geometry& g, dfc* Gt,
                             const dfc* twdf, cudaStream_t st)
 {
     const dim3 grid(g.H / kRowBlock, nframes);
-    const size_t smem = sizeof(dfc) * (g.W + (kRowBlock / 2) * (pad8(g.W) + 1));
+    const size_t smem = row_pass_smem(g.W), smem_max = row_pass_smem(1 << kMaxLog);
     cudaError_t e = cudaSuccess;
     switch (dtype) {
     case 0:
-        if ((e = allow_smem(row_pass_kernel<uint8_t>, smem)) != cudaSuccess) return e;
+        if ((e = allow_smem(row_pass_kernel<uint8_t>, smem_max)) != cudaSuccess) return e;
         row_pass_kernel<uint8_t><<<grid, 256, smem, st>>>((const uint8_t*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf);
         break;
     case 1:
-        if ((e = allow_smem(row_pass_kernel<uint16_t>, smem)) != cudaSuccess) return e;
+        if ((e = allow_smem(row_pass_kernel<uint16_t>, smem_max)) != cudaSuccess) return e;
         row_pass_kernel<uint16_t><<<grid, 256, smem, st>>>((const uint16_t*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf);
         break;
     case 2:
-        if ((e = allow_smem(row_pass_kernel<float>, smem)) != cudaSuccess) return e;
+        if ((e = allow_smem(row_pass_kernel<float>, smem_max)) != cudaSuccess) return e;
         row_pass_kernel<float><<<grid, 256, smem, st>>>((const float*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf);
         break;
     default:
-        if ((e = allow_smem(row_pass_kernel<double>, smem)) != cudaSuccess) return e;
+        if ((e = allow_smem(row_pass_kernel<double>, smem_max)) != cudaSuccess) return e;
         row_pass_kernel<double><<<grid, 256, smem, st>>>((const double*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf);
         break;
     }
@@ -357,9 +365,8 @@ cudaError_t launch_col_pass(int mode, const dfc* Gt, float2* S, const float2* Rb
 {
     const int nchunks = mode == 1 ? 1 : (nframes + fpc - 1) / fpc;
     const dim3 grid(g.hw, nchunks);
-    const size_t smem = sizeof(dfc) * (g.H + kColLines * pad8(g.H))
-                        + sizeof(float2) * (g.H + g.H + kColLines * pad8(g.H)) + sizeof(double) * g.H;
-    cudaError_t e = allow_smem(col_pass_kernel, smem);
+    const size_t smem = col_pass_smem(g.H);
+    cudaError_t e = allow_smem(col_pass_kernel, col_pass_smem(1 << kMaxLog));
     if (e != cudaSuccess)
         return e;
     col_pass_kernel<<<grid, 256, smem, st>>>(mode, Gt, S, Rbuf, Rout, T, Ppart, mode == 1 ? 1 : nframes, fpc,
@@ -380,8 +387,8 @@ cudaError_t launch_xcorr_rows(const float2* T, float* corr, float* rowmax, int n
                               const float2* tw, cudaStream_t st)
 {
     const dim3 grid(g.H / kRowBlock, nframes);
-    const size_t smem = sizeof(float2) * (g.W + g.hw * (kRowBlock + 1) + (kRowBlock / 2) * pad8(g.W));
-    cudaError_t e = allow_smem(xcorr_rows_kernel, smem);
+    const size_t smem = xcorr_rows_smem(g.W);
+    cudaError_t e = allow_smem(xcorr_rows_kernel, xcorr_rows_smem(1 << kMaxLog));
     if (e != cudaSuccess)
         return e;
     xcorr_rows_kernel<<<grid, 256, smem, st>>>(T, corr, rowmax, g.logW, g.H, g.hw, tw);

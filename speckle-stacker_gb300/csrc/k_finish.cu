@@ -120,7 +120,9 @@ cudaError_t launch_finish(const double* Phalf, double pnorm, const double2* phas
     const double trigarg = 6.283185307179586476925286766559 / aperture;
     finish_build_kernel<<<grid_n(n), 256, 0, st>>>(Phalf, pnorm, phases, trigarg, g.W, g.H, Z, power_full); note_launches(1);
     const size_t smem = sizeof(double2) * ((1 << (kTwLog - 1)) + 4 * (size_t)(g.W > g.H ? g.W : g.H));
-    cudaError_t e = cudaFuncSetAttribute(fft_lines_d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the limit is the largest frame's, so that concurrent launches of other shapes never lower it
+    const size_t smem_max = sizeof(double2) * ((1 << (kTwLog - 1)) + 4 * (size_t)(1 << kMaxLog));
+    cudaError_t e = cudaFuncSetAttribute(fft_lines_d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     if (e != cudaSuccess)
         return e;
     // FFTW_BACKWARD over rows (x) then columns (y)

@@ -562,8 +562,12 @@ cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int
     reco_rlist_kernel<<<dim3(256, njobs), 256, 0, st>>>(jobs_dev);
     note_launches(1);
     const size_t smem = (sizeof(float2) + sizeof(int2)) * nv + sizeof(unsigned int) * (((size_t)max_W * max_H + 31) / 32);
-    // the kernel's static shared memory (ring, phase cache) counts against the same 48 KB default
-    cudaError_t e = cudaFuncSetAttribute(phase_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the limit is that of the largest frame and depth (the attribute is per
+    // function; a launch of another shape must never lower it under this one);
+    // the static shared memory (ring, phase cache) counts against it too
+    const size_t smem_max = (sizeof(float2) + sizeof(int2)) * 65 * 65
+                            + sizeof(unsigned int) * (((size_t)1 << (2 * kMaxLog)) / 32);
+    cudaError_t e = cudaFuncSetAttribute(phase_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     if (e != cudaSuccess)
         return e;
     phase_pipe_kernel<<<njobs, kRecoThreads, smem, st>>>(jobs_dev);

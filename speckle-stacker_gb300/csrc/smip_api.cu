@@ -389,6 +389,9 @@ struct smip_stack {
     double2* Z = nullptr;
     double* pfull = nullptr;
     double* maxbuf = nullptr;
+    // phase recovery and the final image: a high-priority stream
+    cudaStream_t rst = nullptr;
+    cudaEvent_t ev_reco = nullptr;
     // smip_batch_launch: this stack's branch of the graph is captured on bst
     cudaStream_t bst = nullptr;
     cudaEvent_t ev_join = nullptr, ev_dep = nullptr;
@@ -398,6 +401,11 @@ struct smip_stack {
         cudaSetDevice(device);
         if (st)
             cudaStreamSynchronize(st);
+        if (rst) {
+            cudaStreamSynchronize(rst);
+            cudaStreamDestroy(rst);
+        }
+        if (ev_reco) cudaEventDestroy(ev_reco);
         if (bst)
             cudaStreamDestroy(bst);
         if (ev_join) cudaEventDestroy(ev_join);
@@ -1041,11 +1049,11 @@ extern "C" int smip_stack_power(smip_stack_t s, double* out)
     return SMIP_OK;
 }
 
-static int normalize_bispec(smip_stack_t s)
+static int normalize_bispec(smip_stack_t s, cudaStream_t q)
 {
     if (!s->Bn)
         CUDA_TRY(cudaMalloc(&s->Bn, sizeof(float2) * s->g.base_size));
-    CUDA_TRY(launch_bispec_normalize(s->B, s->C, (double)s->nframes, s->g.base_size, s->Bn, s->st));
+    CUDA_TRY(launch_bispec_normalize(s->B, s->C, (double)s->nframes, s->g.base_size, s->Bn, q));
     return SMIP_OK;
 }
 
@@ -1054,13 +1062,18 @@ extern "C" int smip_stack_bispectrum(smip_stack_t s, float* out)
     int rc = smip_stack_sync(s);
     if (rc || (rc = need_frames(s)))
         return rc;
-    if ((rc = normalize_bispec(s)))
+    if ((rc = normalize_bispec(s, s->st)))
         return rc;
     CUDA_TRY(cudaMemcpyAsync(out, s->Bn, sizeof(float2) * s->g.base_size, cudaMemcpyDeviceToHost, s->st));
     CUDA_TRY(cudaStreamSynchronize(s->st));
     return SMIP_OK;
 }
 
+// Phase recovery (and the final image) run on the stack's high-priority
+// stream: the walk is one CTA per job, and when several jobs share the GPU
+// its blocks are scheduled ahead of pending accumulation blocks of other
+// jobs.  The stack's stream is idle here (synchronised); rejoin_stream
+// orders the later downloads on it after this work.
 static int stack_reco(smip_stack_t s, double R)
 {
     int rc = smip_stack_sync(s);
@@ -1068,16 +1081,29 @@ static int stack_reco(smip_stack_t s, double R)
         return rc;
     if (!(R >= 0.0))
         return fail(SMIP_E_INVALID_ARGUMENT, "reco_radius must be >= 0");
-    if ((rc = normalize_bispec(s)))
+    if (!s->rst) {
+        int least = 0, greatest = 0;
+        CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CUDA_TRY(cudaStreamCreateWithPriority(&s->rst, cudaStreamNonBlocking, greatest));
+        CUDA_TRY(cudaEventCreateWithFlags(&s->ev_reco, cudaEventDisableTiming));
+    }
+    if ((rc = normalize_bispec(s, s->rst)))
         return rc;
     s->reco.g = s->g;
-    return s->reco.run(s->Bn, R, s->err, s->st);
+    return s->reco.run(s->Bn, R, s->err, s->rst);
+}
+
+static int rejoin_stream(smip_stack_t s)
+{
+    CUDA_TRY(cudaEventRecord(s->ev_reco, s->rst));
+    CUDA_TRY(cudaStreamWaitEvent(s->st, s->ev_reco, 0));
+    return SMIP_OK;
 }
 
 extern "C" int smip_stack_reconstruct(smip_stack_t s, double R, double* phases, unsigned char* flags, double* cons)
 {
     int rc = stack_reco(s, R);
-    if (rc)
+    if (rc || (rc = rejoin_stream(s)))
         return rc;
     if ((rc = s->reco.download(phases, flags, cons, s->st)))
         return rc;
@@ -1100,7 +1126,9 @@ extern "C" int smip_stack_finish(smip_stack_t s, double R, double* image, double
         CUDA_TRY(cudaMalloc(&s->maxbuf, sizeof(double)));
     }
     const double pnorm = (double)((size_t)s->nframes * n);
-    CUDA_TRY(launch_finish(s->P, pnorm, s->reco.phases, 2.0 * R, s->g, s->Z, nullptr, s->maxbuf, s->ctx->tw64, s->st));
+    CUDA_TRY(launch_finish(s->P, pnorm, s->reco.phases, 2.0 * R, s->g, s->Z, nullptr, s->maxbuf, s->ctx->tw64, s->rst));
+    if ((rc = rejoin_stream(s)))
+        return rc;
     if (image)
         CUDA_TRY(cudaMemcpyAsync(image, s->Z, sizeof(double2) * n, cudaMemcpyDeviceToHost, s->st));
     if ((rc = s->reco.download(phases, flags, cons, s->st)))
