@@ -362,18 +362,22 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
             int rc, ta, tb;
             float2 ba, bb;
         };
+        // the list slots are loaded without waiting for the count (a visit's
+        // kRecentMax entries are always allocated) and masked one visit later
         auto load_meta = [&](int q, Ahead& a) {
             if (q >= J.nvisits)
                 return;
             a.w = J.visits[q];
             a.rc = J.rcount[q];
             const unsigned short* rl = J.rlist + (long long)q * kRecentMax;
-            a.ta = lane < a.rc ? (int)rl[lane] : -1;
-            a.tb = lane + 32 < a.rc ? (int)rl[lane + 32] : -1;
+            a.ta = rl[lane];
+            a.tb = rl[lane + 32];
         };
         auto load_plan = [&](int q, Ahead& a) {
             if (q >= J.nvisits)
                 return;
+            a.ta = lane < a.rc ? a.ta : -1;
+            a.tb = lane + 32 < a.rc ? a.tb : -1;
             const float2* prow = J.plan + (long long)q * nv;
             a.ba = a.ta >= 0 ? prow[a.ta] : make_float2(0.f, 0.f);
             a.bb = a.tb >= 0 ? prow[a.tb] : make_float2(0.f, 0.f);
