@@ -13,11 +13,15 @@
 // have no effect (main.cpp:84-90, 136-167 never use them).
 //
 // Input: the reference decodes video/GIF with OpenCV (videoio.h:38-98); here
-// <source> is a NumPy .npy frame stack, uint8/uint16/float32/float64, shape
-// [frames][rows][cols] or [frames][rows][cols][channels].  For a multi-channel
-// stack -c picks channel clamp(round(log2(c)), 0, channels-1) with r=1, g=2,
-// b=4, i=7 (videoio.h:78-79), as Mat2Array does.
+// <source> is an animated GIF (decoded by gif_decode.hpp into BGR frames, the
+// order OpenCV delivers) or a NumPy .npy frame stack, uint8/uint16/float32/
+// float64, shape [frames][rows][cols] or [frames][rows][cols][channels].  For a
+// multi-channel stack -c picks channel clamp(round(log2(c)), 0, channels-1)
+// with r=1, g=2, b=4, i=7 (videoio.h:78-79), as Mat2Array does (so on BGR
+// frames "r" reads the first channel, as the reference's does).
 #include <getopt.h>
+
+#include "gif_decode.hpp"
 
 #include <algorithm>
 #include <array>
@@ -66,7 +70,7 @@ void usage(const char* progname)
               << "     -v   --verbose               :   increase verbosity level\n"
               << "          --version               :   display version and exit\n"
               << "     -h -?  --help                :   help (this screen)\n"
-              << "   <source root>: NumPy .npy frame stack [frames][rows][cols](+[channels]),\n"
+              << "   <source root>: animated GIF, or NumPy .npy frame stack [frames][rows][cols](+[channels]),\n"
               << "                  uint8, uint16, float32 or float64\n\n";
 }
 
@@ -77,6 +81,7 @@ struct Npy {
     int esize = 0;
     std::vector<std::size_t> shape;
     long data_off = 0;
+    std::vector<std::uint8_t> mem; // decoded frames (a GIF), used instead of the file when set
     ~Npy()
     {
         if (f)
@@ -268,9 +273,13 @@ void push_chunk(smip::gpu::Stack& st, Npy& n, std::size_t first, std::size_t cou
     const std::size_t ch = n.shape.size() == 4 ? n.shape[3] : 1;
     const std::size_t fe = rows * cols * ch;
     std::vector<T> in(fe * count);
-    std::fseek(n.f, n.data_off + (long)(first * fe * sizeof(T)), SEEK_SET);
-    if (std::fread(in.data(), sizeof(T), in.size(), n.f) != in.size())
-        throw std::runtime_error("error reading frames");
+    if (!n.mem.empty()) {
+        std::memcpy(in.data(), n.mem.data() + first * fe * sizeof(T), in.size() * sizeof(T));
+    } else {
+        std::fseek(n.f, n.data_off + (long)(first * fe * sizeof(T)), SEEK_SET);
+        if (std::fread(in.data(), sizeof(T), in.size(), n.f) != in.size())
+            throw std::runtime_error("error reading frames");
+    }
     if (ch == 1) {
         st.push_frames(in.data(), count);
         return;
@@ -373,7 +382,16 @@ int main(int argc, char* argv[])
         const std::string filename(*argv);
 
         Npy npy;
-        open_npy(npy, filename);
+        if (smipcli::is_gif(filename)) {
+            // animated GIF: frames in BGR, as OpenCV's VideoCapture delivers them
+            smipcli::GifFrames gf = smipcli::read_gif(filename, max_frames);
+            npy.kind = 'u';
+            npy.esize = 1;
+            npy.shape = { gf.count, gf.height, gf.width, 3 };
+            npy.mem = std::move(gf.bgr);
+        } else {
+            open_npy(npy, filename);
+        }
         info() << "opened frame stack " << filename << ": " << npy.shape[0] << " frames\n";
         const std::size_t nframes = std::min<std::size_t>(npy.shape[0], max_frames);
         notice() << "using " << nframes << "/" << npy.shape[0] << " frames\n";

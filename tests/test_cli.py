@@ -153,3 +153,29 @@ def test_cpp_layer_matches_binding(smip, tmp_path):
     assert np.array_equal(np.fromfile(tmp_path / "stack_flags.bin", np.uint8), fl.ravel())
     assert tuple(np.fromfile(tmp_path / "next_reco.bin", np.int32)) == smip.next_reco_index(0.0, 0.0, 0, 0)[2:]
     assert np.array_equal(np.fromfile(tmp_path / "hann.bin", np.float64), smip.hann(64, 64, 48.0).ravel())
+
+
+@pytest.mark.gpu
+def test_cli_reads_animated_gif(smip, tmp_path):
+    """An animated GIF through smip-cli equals the same frames given as .npy:
+    frames in BGR as OpenCV delivers them, -c r reading channel 0 (blue) and
+    -c b channel 2 (red), as Mat2Array's channel = round(log2(c)) does."""
+    _need_cli()
+    from smip_gb300 import synthetic as S
+    from test_gif import write_gif
+
+    idx = S.make_stack(S.config_spec("binary128", nframes=8, n=64)).astype(np.int64)  # u8 values as palette indices
+    pal = np.stack([np.arange(256), 255 - np.arange(256), (np.arange(256) * 7) % 256], axis=1)  # R, G, B
+    gif = tmp_path / "stack.gif"
+    write_gif(str(gif), 64, 64, [{"idx": f, "disposal": 1} for f in idx], gct=pal)
+    for flag, plane in (("r", pal[:, 2]), ("b", pal[:, 0])):
+        d_gif, d_npy = tmp_path / f"gif_{flag}", tmp_path / f"npy_{flag}"
+        d_gif.mkdir()
+        d_npy.mkdir()
+        np.save(d_npy / "stack.npy", plane[idx].astype(np.uint8))
+        for d, src in ((d_gif, gif), (d_npy, d_npy / "stack.npy")):
+            r = subprocess.run([CLI, "-b", "16", "-p", "20", "-c", flag, str(src)], capture_output=True, text=True,
+                               cwd=d)
+            assert r.returncode == 0, r.stderr
+        assert open(d_gif / "bispectrum.dat", "rb").read() == open(d_npy / "bispectrum.dat", "rb").read()
+        assert np.array_equal(read_png16(d_gif / "sum_image.png"), read_png16(d_npy / "sum_image.png"))
