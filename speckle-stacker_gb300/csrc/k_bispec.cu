@@ -32,8 +32,10 @@
 // forms would need either register moves on the same pipe or twice the
 // shared-memory bytes, and either costs more than it saves.
 //
-// Per frame, three TMA box loads from the S[f][a][c] spectrum layout
-// (k_fft.cu; 8-byte elements) fill one stage of a shared-memory ring:
+// Per ring stage, three TMA box loads from the S[f][a][c] spectrum layout
+// (k_fft.cu; 8-byte elements) bring FPS = 4 frames (the box's outermost
+// dimension), so the wait, the release and the stage's address arithmetic
+// are paid once per four frames:
 //   W box: rows a0 + a2, columns j + l + H/2   -> F(u+v)
 //   V box: rows a2,      columns l + H/2       -> F(v)
 //   A box: row a0,       columns j + H/2       -> F(u)  (row-0 tiles read F(u)

@@ -160,37 +160,9 @@ __device__ __forceinline__ dfc df_cmul(const dfc& a, const dfc& w)
     return r;
 }
 
-// In-place radix-2 DIT float-float FFT (same contract as fft_stages).
-__device__ inline void df_fft_stages(dfc* buf, int logn, int nl, int ls, const dfc* tw, int twlog, int sign)
-{
-    const int n = 1 << logn;
-    const int nb = nl * (n >> 1);
-    for (int s = 1; s <= logn; ++s) {
-        const int half = 1 << (s - 1);
-        const int tsh = twlog - s;
-        for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-            const int line = b >> (logn - 1);
-            const int q = b & ((n >> 1) - 1);
-            const int k = q & (half - 1);
-            const int i0 = ((q >> (s - 1)) << s) + k;
-            dfc w = tw[k << tsh];
-            if (sign > 0) {
-                w.h.y = -w.h.y;
-                w.l.y = -w.l.y;
-            }
-            dfc* L = buf + line * ls;
-            const dfc a = L[i0];
-            const dfc t = df_cmul(L[i0 + half], w);
-            L[i0] = df_cadd(a, t);
-            L[i0 + half] = df_csub(a, t);
-        }
-        __syncthreads();
-    }
-}
-
 // ------------------------------------------ register-staged radix-2 passes
-// Same transform, twiddles and per-butterfly arithmetic as fft_stages /
-// df_fft_stages (so results are bit-identical), but a thread loads the 2^K
+// The radix-2 DIT transform of fft_stages (same twiddle values and
+// per-butterfly arithmetic, float2 or float-float), but a thread loads the 2^K
 // elements that K consecutive stages combine, runs those stages in registers
 // and stores once: one shared-memory round trip and one __syncthreads per
 // pass of up to 3 stages instead of per stage.  Lines are stored padded, one
