@@ -57,6 +57,10 @@ namespace smip_gpu {
 
 constexpr uint64_t kWaitNs = 2000000000ull; // 2 s
 
+// Resident CTAs per SM, each with its own ring.  Two CTAs of 8 warps measured
+// the same as one of 16 (189.5k vs 189.7k frames/s at 256x256, d = 32).
+constexpr int kCtasPerSm = 1;
+
 template <int DE>
 struct BCfg {
     static constexpr int ROWS = DE / 2;                    // main rows a2 = 1..d/2
@@ -64,7 +68,7 @@ struct BCfg {
     static constexpr int NLB = (TL + 3) / 4;               // l blocks per row
     static constexpr int TLW = (TL + NLB - 1) / NLB;       // l groups per block
     static constexpr int RPC = (NLB == 1 && ROWS % 8 == 0) ? 8 : 4; // rows (a0 for row-0 tiles) per tile
-    static constexpr int WARPS = 16;
+    static constexpr int WARPS = 16 / kCtasPerSm;
     static constexpr int NJB = WARPS / (RPC * NLB);        // 32-wide j blocks per tile
     static constexpr int JT = 32 * NJB;                    // tile j width
     static constexpr int THREADS = WARPS * 32;
@@ -79,13 +83,13 @@ struct BCfg {
     static constexpr int VOFF = (FPS * WBYTES + 127) / 128 * 128;
     static constexpr int AOFF = VOFF + (FPS * VBYTES + 127) / 128 * 128;
     static constexpr int STAGE = AOFF + (FPS * ABYTES + 127) / 128 * 128;
-    static constexpr int NSR = (200 * 1024) / STAGE;       // ~200 KB of frame stages
+    static constexpr int NSR = (200 * 1024 / kCtasPerSm) / STAGE; // ~200 KB of frame stages per SM
     static constexpr int NS = NSR > 16 ? 16 : (NSR < 4 ? 4 : NSR);
     static constexpr int LAG = 2;                          // iterations between a stage's release and its refill
                                                            // (3 at d = 32, with 6 stages, measured no faster)
     static constexpr int SMEM = NS * STAGE + 2 * NS * 8 + 16;
     static_assert(RPC * NLB * NJB == WARPS && ROWS % RPC == 0, "task split");
-    static_assert(BW <= 256 && NS > LAG + 1 && SMEM <= 227 * 1024, "box / ring");
+    static_assert(BW <= 256 && NS > LAG + 1 && SMEM <= (227 * 1024) / kCtasPerSm - 1024, "box / ring");
 };
 
 struct BispecArgs {
@@ -177,7 +181,7 @@ __device__ __forceinline__ void cmac(float2& acc, float2 a, float2 v, float2 w)
 // EXACT: the stack's depth is DE itself (compile-time layout); otherwise the
 // depth comes from the arguments (BispecArgs::D < DE).
 template <int DE, bool EXACT>
-__global__ void __launch_bounds__(BCfg<DE>::THREADS, 1)
+__global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
     bispec_accum_kernel(const __grid_constant__ CUtensorMap tmW, const __grid_constant__ CUtensorMap tmV,
                         const __grid_constant__ CUtensorMap tmA, const BispecArgs p)
 {
@@ -549,7 +553,7 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
     // on whichever SMs are free, also while other streams' kernels run).  The
     // tiles of the last partial wave (one CTA per SM) are split by frames so
     // that the wave is full (parts of at least 8 frames).
-    const int G = L.num_sms;
+    const int G = L.num_sms * kCtasPerSm; // CTAs of one full wave
     const int rem = a.ntiles % G;
     int P = rem > 0 ? G / rem : 1;
     P = P < 1 ? 1 : P;
@@ -570,7 +574,8 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
 bool bispec_depth_supported(int De) { return De >= 2 && De <= 64 && De % 2 == 0; }
 
 // partial sums of one split-tile part: (8 j x 4 l + 1 edge) float2 per thread, 512 threads
-size_t bispec_scratch_bytes(int num_sms) { return (size_t)num_sms * 33 * 512 * sizeof(float2); }
+size_t bispec_scratch_bytes(int num_sms) { return (size_t)num_sms * kCtasPerSm * 33 * (512 / kCtasPerSm) * sizeof(float2); }
+size_t bispec_tile_counters(int num_sms) { return (size_t)num_sms * kCtasPerSm; }
 
 // The kernel is instantiated for depths that are multiples of 8; another even
 // depth runs the next one up and stores only its own elements.

@@ -520,8 +520,8 @@ struct smip_stack {
         }
         if (!kscratch) {
             CUDA_TRY(cudaMalloc(&kscratch, bispec_scratch_bytes(ctx->num_sms)));
-            CUDA_TRY(cudaMalloc(&ktile_cnt, sizeof(int) * ctx->num_sms));
-            CUDA_TRY(cudaMemsetAsync(ktile_cnt, 0, sizeof(int) * ctx->num_sms, st));
+            CUDA_TRY(cudaMalloc(&ktile_cnt, sizeof(int) * bispec_tile_counters(ctx->num_sms)));
+            CUDA_TRY(cudaMemsetAsync(ktile_cnt, 0, sizeof(int) * bispec_tile_counters(ctx->num_sms), st));
         }
         return SMIP_OK;
     }
@@ -798,7 +798,7 @@ extern "C" int smip_stack_reset(smip_stack_t s)
     CUDA_TRY(cudaMemsetAsync(s->sum, 0, 8 * s->frame_elems(), s->st));
     CUDA_TRY(cudaMemsetAsync(s->err, 0, sizeof(int), s->st));
     if (s->ktile_cnt) // a launch that stopped early (timeout) may leave parts counted
-        CUDA_TRY(cudaMemsetAsync(s->ktile_cnt, 0, sizeof(int) * s->ctx->num_sms, s->st));
+        CUDA_TRY(cudaMemsetAsync(s->ktile_cnt, 0, sizeof(int) * bispec_tile_counters(s->ctx->num_sms), s->st));
     s->nframes = 0;
     s->pending = 0;
     s->has_ref = false;

@@ -84,10 +84,11 @@ struct BispecLaunch {
     int* err;
     int num_sms;
     float2* scratch;     // bispec_scratch_bytes(num_sms): partial sums of split tiles
-    int* tile_cnt;       // num_sms ints, zeroed once: parts finished per split tile
+    int* tile_cnt;       // bispec_tile_counters(num_sms) ints, zeroed once: parts finished per split tile
 };
 cudaError_t launch_bispec_accumulate(const BispecLaunch& L, const Geometry& g, cudaStream_t st);
 size_t bispec_scratch_bytes(int num_sms);
+size_t bispec_tile_counters(int num_sms);
 bool bispec_depth_supported(int De);
 
 // out = (B - C) / nframes  (float2 packed), or plain add dst += src for merge.
