@@ -117,6 +117,14 @@ SMIP_GPU_API int smip_stack_sync(smip_stack_t s);
  * this is the graph-captured many-stack launch the serving loop uses. */
 SMIP_GPU_API int smip_batch_launch(smip_stack_t* stacks, long count);
 
+/* Diagnostic of the failure path: runs a kernel whose two waits (an mbarrier
+ * nothing arrives on, a device flag nothing sets) can never be satisfied.
+ * Both give up after timeout_s seconds (at most 10), record the expiry and
+ * return, so the call returns SMIP_E_TIMEOUT -- what any call reports after a
+ * bounded device wait expired -- and the device stays usable.  No counterpart
+ * in the reference (its loops are host code). */
+SMIP_GPU_API int smip_diag_bounded_wait(int device, double timeout_s);
+
 SMIP_GPU_API int smip_stack_frame_count(smip_stack_t s, long* nframes);
 SMIP_GPU_API int smip_stack_bispectrum_size(smip_stack_t s, long* base_size);
 

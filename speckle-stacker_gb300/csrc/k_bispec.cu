@@ -597,6 +597,41 @@ cudaError_t launch_bispec_accumulate(const BispecLaunch& L, const Geometry& g, c
     }
 }
 
+// ------------------------------------------------ bounded-wait diagnostic
+// The failure path every kernel takes when a wait expires, run on purpose:
+// block 0 waits (bounded, as the bispectrum kernel's ring does) on an mbarrier
+// that nothing arrives on; block 1 polls (bounded, as the phase walk does) a
+// global flag that nothing sets.  Both record SMIP_DEV_ERR_TIMEOUT and return;
+// no copy is in flight and nothing else waits on them.
+__global__ void bounded_wait_probe_kernel(int* err, unsigned long long timeout_ns, const int* never)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (blockIdx.x == 0) {
+        if (threadIdx.x == 0) {
+            mbar_init(&bar, 1);
+            fence_mbar_init();
+        }
+        __syncthreads();
+        const bool got = mbar_wait_bounded(&bar, 0, timeout_ns);
+        if (!__all_sync(0xffffffffu, got) && threadIdx.x == 0)
+            record_error(err, SMIP_DEV_ERR_TIMEOUT);
+    } else {
+        const unsigned long long t0 = globaltimer_ns();
+        bool got = false;
+        while (!(got = *reinterpret_cast<const volatile int*>(never) != 0) && globaltimer_ns() - t0 <= timeout_ns) {
+        }
+        if (!got && threadIdx.x == 0)
+            record_error(err, SMIP_DEV_ERR_TIMEOUT);
+    }
+}
+
+cudaError_t launch_bounded_wait_probe(int* err, const int* never, double timeout_s, cudaStream_t st)
+{
+    bounded_wait_probe_kernel<<<2, 32, 0, st>>>(err, (unsigned long long)(timeout_s * 1e9), never);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------- normalise, merge
 // (B - C) / n: the difference is exact in FP64; a multiply by 1/n instead of
 // a divide keeps the FP64 pipe's share small (GB300's FP64 rate is low).

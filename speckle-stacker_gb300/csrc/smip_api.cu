@@ -969,6 +969,31 @@ extern "C" int smip_batch_launch(smip_stack_t* stacks, long count)
     return SMIP_OK;
 }
 
+extern "C" int smip_diag_bounded_wait(int device, double timeout_s)
+{
+    if (!(timeout_s > 0.0 && timeout_s <= 10.0))
+        return fail(SMIP_E_INVALID_ARGUMENT, "timeout must be in (0, 10] s");
+    CUDA_TRY(cudaSetDevice(device));
+    cudaStream_t st = nullptr;
+    int* buf = nullptr; // [0] device error word, [1] the flag nothing sets
+    CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    int rc = SMIP_OK;
+    cudaError_t e = cudaMalloc(&buf, 2 * sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMemsetAsync(buf, 0, 2 * sizeof(int), st);
+    if (e == cudaSuccess)
+        e = launch_bounded_wait_probe(buf, buf + 1, timeout_s, st);
+    if (e != cudaSuccess)
+        rc = fail(SMIP_E_CUDA, cudaGetErrorString(e));
+    else
+        rc = check_dev_err(buf, st); // SMIP_E_TIMEOUT, as after any expired wait
+    cudaStreamSynchronize(st);
+    if (buf)
+        cudaFree(buf);
+    cudaStreamDestroy(st);
+    return rc;
+}
+
 extern "C" int smip_stack_frame_count(smip_stack_t s, long* n)
 {
     int rc = check_stack(s);

@@ -88,6 +88,8 @@ struct BispecLaunch {
 };
 cudaError_t launch_bispec_accumulate(const BispecLaunch& L, const Geometry& g, cudaStream_t st);
 size_t bispec_scratch_bytes(int num_sms);
+// diagnostic: two bounded waits that can never be satisfied (see smip_diag_bounded_wait)
+cudaError_t launch_bounded_wait_probe(int* err, const int* never, double timeout_s, cudaStream_t st);
 size_t bispec_tile_counters(int num_sms);
 bool bispec_depth_supported(int De);
 

@@ -104,6 +104,7 @@ def _load():
         "smip_stack_finish": ([vp, C.c_double, dp, dp, ubp, dp], C.c_int),
         "smip_stack_merge": ([vp, vp], C.c_int),
         "smip_batch_launch": ([C.POINTER(vp), C.c_long], C.c_int),
+        "smip_diag_bounded_wait": ([C.c_int, C.c_double], C.c_int),
         "smip_stack_share_reference": ([vp, vp], C.c_int),
         "smip_stack_save_bispectrum": ([vp, C.c_char_p], C.c_int),
         "smip_stack_load_bispectrum": ([vp, C.c_char_p, C.c_long], C.c_int),
@@ -161,6 +162,12 @@ def batch_launch(stacks) -> None:
     stacks = list(stacks)
     arr = (C.c_void_p * max(1, len(stacks)))(*[st._h.value for st in stacks])
     _check(_L().smip_batch_launch(arr, len(stacks)))
+
+
+def diag_bounded_wait(device: int = 0, timeout_s: float = 0.05) -> None:
+    """Runs a kernel whose bounded waits can never be satisfied; raises
+    DeviceTimeout, as any call does after an expired device wait."""
+    _check(_L().smip_diag_bounded_wait(device, float(timeout_s)))
 
 
 def kernel_launches() -> int:
