@@ -178,6 +178,11 @@ SMIP_GPU_API int smip_stack_save_bispectrum(smip_stack_t s, const char* path);
  * SMIP_E_RUNTIME on I/O errors, SMIP_E_INVALID_ARGUMENT on a shape mismatch. */
 SMIP_GPU_API int smip_stack_load_bispectrum(smip_stack_t s, const char* path, long nframes);
 
+/* smip_stack_load_bispectrum from memory: bispec holds base_size normalised
+ * complex<float> in the packed layout smip_stack_bispectrum returns (the data
+ * block of bispectrum.dat, bispectrum.h:442-461); the stack must be empty. */
+SMIP_GPU_API int smip_stack_set_bispectrum(smip_stack_t s, const float* bispec, long nframes);
+
 /* ========================================================================== *
  * Standalone calls mirroring the reference's free functions and classes.
  * ========================================================================== */

@@ -1291,14 +1291,32 @@ extern "C" int smip_stack_load_bispectrum(smip_stack_t s, const char* path, long
     std::fclose(f);
     if (!ok)
         return fail(SMIP_E_RUNTIME, std::string("error reading data block from file ") + path);
-    // the file holds the normalised bispectrum: the accumulator resumes as
-    // file x nframes with zero compensation, over nframes frames
+    return smip_stack_set_bispectrum(s, buf.data(), nframes);
+}
+
+extern "C" int smip_stack_set_bispectrum(smip_stack_t s, const float* bispec, long nframes)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    if (!bispec)
+        return fail(SMIP_E_INVALID_ARGUMENT, "null bispectrum");
+    if (s->nframes != 0)
+        return fail(SMIP_E_INVALID_ARGUMENT, "stack already holds frames; reset it before loading a bispectrum");
+    const size_t n = (size_t)s->g.base_size;
+    // the normalised bispectrum: the accumulator resumes as it x nframes with
+    // zero compensation, over nframes frames
     const long nf = nframes > 0 ? nframes : 1;
-    if (nf != 1)
+    std::vector<float> buf;
+    const float* src = bispec;
+    if (nf != 1) {
+        buf.assign(bispec, bispec + 2 * n);
         for (float& v : buf)
             v = (float)((double)v * (double)nf);
+        src = buf.data();
+    }
     CUDA_TRY(cudaStreamSynchronize(s->st));
-    CUDA_TRY(cudaMemcpy(s->B, buf.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(s->B, src, sizeof(float2) * n, cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMemset(s->C, 0, sizeof(float2) * n));
     s->nframes = nf;
     s->pending = 0;

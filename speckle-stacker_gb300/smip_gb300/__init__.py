@@ -105,6 +105,7 @@ def _load():
         "smip_stack_merge": ([vp, vp], C.c_int),
         "smip_batch_launch": ([C.POINTER(vp), C.c_long], C.c_int),
         "smip_diag_bounded_wait": ([C.c_int, C.c_double], C.c_int),
+        "smip_stack_set_bispectrum": ([vp, fp, C.c_long], C.c_int),
         "smip_stack_share_reference": ([vp, vp], C.c_int),
         "smip_stack_save_bispectrum": ([vp, C.c_char_p], C.c_int),
         "smip_stack_load_bispectrum": ([vp, C.c_char_p, C.c_long], C.c_int),
@@ -341,6 +342,14 @@ class Stack:
         stack: the accumulator resumes as the file's normalised bispectrum x
         nframes (0 = 1); reconstruct_phases and accumulate_from_fft work on it."""
         _check(_L().smip_stack_load_bispectrum(self._h, path.encode(), int(nframes)))
+
+    def set_bispectrum(self, bispec, nframes: int = 0):
+        """load_bispectrum from memory: a complex64 array of base_size, the
+        packed normalised bispectrum (what bispectrum() returns)."""
+        b = np.ascontiguousarray(bispec, np.complex64).ravel()
+        if b.size != self.base_size:
+            raise InvalidArgument(f"bispectrum has {b.size} elements, the stack {self.base_size}")
+        _check(_L().smip_stack_set_bispectrum(self._h, b.ctypes.data_as(C.POINTER(C.c_float)), int(nframes)))
 
 
 # ------------------------------------------------------- free functions

@@ -305,6 +305,11 @@ def test_load_bispectrum_resume(smip, tmp_path):
         assert rel_l2(c.bispectrum(), b6) <= 1e-6
         with pytest.raises(smip.InvalidArgument):
             c.push_frames(np.zeros((1, H, W), np.uint16))
+    with smip.Stack(W, H, D) as m:  # the same from memory
+        m.set_bispectrum(b4)
+        assert np.array_equal(m.bispectrum(), b4)
+        ph_m, fl_m, _ = m.reconstruct_phases(20)
+        assert np.array_equal(fl_m, fl_a) and np.array_equal(ph_m, ph_a)
     with smip.Stack(W, H, 24) as d, pytest.raises(smip.InvalidArgument):
         d.load_bispectrum(fn)
     with smip.Stack(W, H, D) as e, pytest.raises(smip.RuntimeFailure):
