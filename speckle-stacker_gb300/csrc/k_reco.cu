@@ -465,8 +465,8 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
                 }
                 __syncwarp();
             }
-            // publish progress every 8 visits: one fence (which waits for the
-            // phase-map stores) per 8 visits; the lag leaves the slack
+            // publish progress every 8 visits (a release store; the lag leaves
+            // the slack)
             if (((q & 7) == 7 || q + 1 == J.nvisits) && lane == 0)
                 st_release_cta(&progress, q + 1);
             __syncwarp();
