@@ -178,6 +178,15 @@ SMIP_GPU_API int smip_stack_save_bispectrum(smip_stack_t s, const char* path);
  * SMIP_E_RUNTIME on I/O errors, SMIP_E_INVALID_ARGUMENT on a shape mismatch. */
 SMIP_GPU_API int smip_stack_load_bispectrum(smip_stack_t s, const char* path, long nframes);
 
+/* Whole-stack checkpoint of a served job (no counterpart in the reference,
+ * whose only persistence is bispectrum.dat): after a flush, the accumulators
+ * (bispectrum and its compensation, power spectrum, shift-and-add sum), the
+ * shifts so far and the reference frame with its spectrum.  Loading it into an
+ * empty stack of the same shape resumes the job: frames pushed afterwards give
+ * what pushing them into the original stack would have given. */
+SMIP_GPU_API int smip_stack_save_state(smip_stack_t s, const char* path);
+SMIP_GPU_API int smip_stack_load_state(smip_stack_t s, const char* path);
+
 /* smip_stack_load_bispectrum from memory: bispec holds base_size normalised
  * complex<float> in the packed layout smip_stack_bispectrum returns (the data
  * block of bispectrum.dat, bispectrum.h:442-461); the stack must be empty. */

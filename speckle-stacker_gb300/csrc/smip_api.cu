@@ -1262,6 +1262,127 @@ extern "C" int smip_stack_save_bispectrum(smip_stack_t s, const char* path)
     return SMIP_OK;
 }
 
+// ------------------------------------------------- full stack checkpoint
+// bispectrum.dat keeps the reference's format (the normalised bispectrum
+// only).  A served job that stops and resumes needs the whole accumulator
+// state; this file holds it, after a flush:
+//   "SMIPSTK1", int32 W, H, De, dtype, mode, has_ref, int64 nframes, base_size,
+//   B, C [base_size] float2, P [hw*H] f64, sum [W*H] 8-byte, shifts [nframes] int2,
+//   and for frames: ref frame [W*H] in dtype, ref_sq f64, R [hw*H] float2.
+namespace {
+bool put(FILE* f, const void* p, size_t n) { return n == 0 || std::fwrite(p, 1, n, f) == n; }
+bool get(FILE* f, void* p, size_t n) { return n == 0 || std::fread(p, 1, n, f) == n; }
+int dev_to_file(FILE* f, const void* d, size_t n, cudaStream_t st)
+{
+    std::vector<unsigned char> h(n);
+    if (n) {
+        CUDA_TRY(cudaMemcpyAsync(h.data(), d, n, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    return put(f, h.data(), n) ? SMIP_OK : fail(SMIP_E_RUNTIME, "error writing the stack state");
+}
+int file_to_dev(FILE* f, void* d, size_t n)
+{
+    std::vector<unsigned char> h(n);
+    if (!get(f, h.data(), n))
+        return fail(SMIP_E_RUNTIME, "error reading the stack state");
+    if (n)
+        CUDA_TRY(cudaMemcpy(d, h.data(), n, cudaMemcpyHostToDevice));
+    return SMIP_OK;
+}
+} // namespace
+
+extern "C" int smip_stack_save_state(smip_stack_t s, const char* path)
+{
+    int rc = smip_stack_sync(s); // flushes the pending batch
+    if (rc)
+        return rc;
+    if (!path)
+        return fail(SMIP_E_INVALID_ARGUMENT, "null path");
+    FILE* f = std::fopen(path, "wb");
+    if (!f)
+        return fail(SMIP_E_RUNTIME, std::string("unable to open file ") + path + " for writing");
+    const int32_t hdr[6] = { s->g.W, s->g.H, s->g.De, s->dtype, s->mode, s->has_ref ? 1 : 0 };
+    const int64_t cnt[2] = { s->nframes, s->g.base_size };
+    const size_t bs = (size_t)s->g.base_size, he = s->half_elems(), fe = s->frame_elems();
+    bool ok = put(f, "SMIPSTK1", 8) && put(f, hdr, sizeof hdr) && put(f, cnt, sizeof cnt);
+    rc = ok ? SMIP_OK : fail(SMIP_E_RUNTIME, "error writing the stack state");
+    if (!rc) rc = dev_to_file(f, s->B, sizeof(float2) * bs, s->st);
+    if (!rc) rc = dev_to_file(f, s->C, sizeof(float2) * bs, s->st);
+    if (!rc) rc = dev_to_file(f, s->P, sizeof(double) * he, s->st);
+    if (!rc) rc = dev_to_file(f, s->sum, 8 * fe, s->st);
+    if (!rc && s->mode == 1) {
+        rc = dev_to_file(f, s->shifts, sizeof(int) * 2 * (size_t)s->nframes, s->st);
+        if (!rc) rc = dev_to_file(f, s->ref, dtype_size(s->dtype) * fe, s->st);
+        if (!rc) rc = dev_to_file(f, s->ref_sq, sizeof(double), s->st);
+        if (!rc) rc = dev_to_file(f, s->R, sizeof(float2) * he, s->st);
+    }
+    std::fclose(f);
+    return rc;
+}
+
+extern "C" int smip_stack_load_state(smip_stack_t s, const char* path)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    if (!path)
+        return fail(SMIP_E_INVALID_ARGUMENT, "null path");
+    if (s->nframes != 0)
+        return fail(SMIP_E_INVALID_ARGUMENT, "stack already holds frames; reset it before loading a state");
+    FILE* f = std::fopen(path, "rb");
+    if (!f)
+        return fail(SMIP_E_RUNTIME, std::string("unable to open file ") + path);
+    char magic[8];
+    int32_t hdr[6];
+    int64_t cnt[2];
+    if (!get(f, magic, 8) || std::memcmp(magic, "SMIPSTK1", 8) != 0 || !get(f, hdr, sizeof hdr) || !get(f, cnt, sizeof cnt)) {
+        std::fclose(f);
+        return fail(SMIP_E_RUNTIME, std::string(path) + ": not a stack state file");
+    }
+    const int dtype = hdr[3], mode = hdr[4];
+    if (hdr[0] != s->g.W || hdr[1] != s->g.H || hdr[2] != s->g.De || cnt[1] != s->g.base_size
+        || (mode == 1 && !dtype_size(dtype)) || mode < 0 || mode > 2 || cnt[0] < 0) {
+        std::fclose(f);
+        return fail(SMIP_E_INVALID_ARGUMENT, std::string("stack state ") + path + " has another shape than the stack");
+    }
+    const size_t bs = (size_t)s->g.base_size, he = s->half_elems(), fe = s->frame_elems();
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    rc = file_to_dev(f, s->B, sizeof(float2) * bs);
+    if (!rc) rc = file_to_dev(f, s->C, sizeof(float2) * bs);
+    if (!rc) rc = file_to_dev(f, s->P, sizeof(double) * he);
+    if (!rc) rc = file_to_dev(f, s->sum, 8 * fe);
+    if (!rc && mode == 1) {
+        if (s->dtype >= 0 && s->dtype != dtype) { // buffers sized for another element type
+            s->free_staging();
+            cudaFree(s->ref);
+            s->ref = nullptr;
+            s->dtype = -1;
+        }
+        if (s->dtype < 0) {
+            if ((rc = s->ensure_staging(dtype_size(dtype) * fe)) == SMIP_OK) {
+                if (cudaMalloc(&s->ref, dtype_size(dtype) * fe) != cudaSuccess)
+                    rc = fail(SMIP_E_NO_MEMORY, "cudaMalloc failed");
+                else
+                    s->dtype = dtype;
+            }
+        }
+        if (!rc) rc = s->ensure_shift_cap(cnt[0]);
+        if (!rc) rc = file_to_dev(f, s->shifts, sizeof(int) * 2 * (size_t)cnt[0]);
+        if (!rc) rc = file_to_dev(f, s->ref, dtype_size(dtype) * fe);
+        if (!rc) rc = file_to_dev(f, s->ref_sq, sizeof(double));
+        if (!rc) rc = file_to_dev(f, s->R, sizeof(float2) * he);
+    }
+    std::fclose(f);
+    if (rc)
+        return rc;
+    s->nframes = cnt[0];
+    s->pending = 0;
+    s->mode = mode;
+    s->has_ref = hdr[5] != 0;
+    return SMIP_OK;
+}
+
 extern "C" int smip_stack_load_bispectrum(smip_stack_t s, const char* path, long nframes)
 {
     int rc = check_stack(s);

@@ -106,6 +106,8 @@ def _load():
         "smip_batch_launch": ([C.POINTER(vp), C.c_long], C.c_int),
         "smip_diag_bounded_wait": ([C.c_int, C.c_double], C.c_int),
         "smip_stack_set_bispectrum": ([vp, fp, C.c_long], C.c_int),
+        "smip_stack_save_state": ([vp, C.c_char_p], C.c_int),
+        "smip_stack_load_state": ([vp, C.c_char_p], C.c_int),
         "smip_stack_share_reference": ([vp, vp], C.c_int),
         "smip_stack_save_bispectrum": ([vp, C.c_char_p], C.c_int),
         "smip_stack_load_bispectrum": ([vp, C.c_char_p, C.c_long], C.c_int),
@@ -342,6 +344,14 @@ class Stack:
         stack: the accumulator resumes as the file's normalised bispectrum x
         nframes (0 = 1); reconstruct_phases and accumulate_from_fft work on it."""
         _check(_L().smip_stack_load_bispectrum(self._h, path.encode(), int(nframes)))
+
+    def save_state(self, path: str):
+        """Whole-stack checkpoint (after a flush): accumulators, shifts and the
+        reference frame; load_state on an empty stack of the same shape resumes."""
+        _check(_L().smip_stack_save_state(self._h, path.encode()))
+
+    def load_state(self, path: str):
+        _check(_L().smip_stack_load_state(self._h, path.encode()))
 
     def set_bispectrum(self, bispec, nframes: int = 0):
         """load_bispectrum from memory: a complex64 array of base_size, the
