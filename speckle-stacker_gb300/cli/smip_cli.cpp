@@ -12,6 +12,15 @@
 // reference, -r, -k, -s, --no-calcsum and --no-specklemasking are parsed and
 // have no effect (main.cpp:84-90, 136-167 never use them).
 //
+// --apply-ignored (not a reference flag) makes them take effect as their help
+// text describes: -r idx makes frame idx the cross-correlation reference (it
+// is accumulated first, then the others in order); -k l:t and -s w:h crop
+// every frame to that box before ingest (the box must lie inside the frame;
+// its size follows the stack's power-of-two rule); --no-calcsum leaves out the
+// sum images; --no-specklemasking leaves out bispectrum.dat, the phase
+// reconstruction and the images made from it.  -f (follow) is not parsed by
+// the reference (getopt prints the usage) and is not here either.
+//
 // Input: the reference decodes video/GIF with OpenCV (videoio.h:38-98); here
 // <source> is an animated GIF (decoded by gif_decode.hpp into BGR frames, the
 // order OpenCV delivers) or a NumPy .npy frame stack, uint8/uint16/float32/
@@ -68,6 +77,8 @@ void usage(const char* progname)
               << "     -k   --croppos <l:t>         :   fixed crop box position (default: 0:0)\n"
               << "     -s   --cropsize <w:h>        :   crop box size (default: total image)\n"
               << "     -v   --verbose               :   increase verbosity level\n"
+              << "          --apply-ignored         :   make -r, -k, -s, --no-calcsum and --no-specklemasking\n"
+              << "                                      take effect (the reference parses and ignores them)\n"
               << "          --version               :   display version and exit\n"
               << "     -h -?  --help                :   help (this screen)\n"
               << "   <source root>: animated GIF, or NumPy .npy frame stack [frames][rows][cols](+[channels]),\n"
@@ -266,28 +277,37 @@ void save_image(const std::string& path, std::size_t w, std::size_t h, F value, 
     write_png16(path, w, h, colour ? 3 : 1, px);
 }
 
+// Crop box of the frames handed to the stack: columns [l, l + w), rows [t, t + h).
+struct Crop {
+    std::size_t l = 0, t = 0, w = 0, h = 0;
+};
+
+// Pushes frames order[first, first + count) of the source, channel `channel`,
+// cut to the crop box.
 template <class T>
-void push_chunk(smip::gpu::Stack& st, Npy& n, std::size_t first, std::size_t count, std::size_t channel)
+void push_chunk(smip::gpu::Stack& st, Npy& n, const std::vector<std::size_t>& order, std::size_t first,
+                std::size_t count, std::size_t channel, const Crop& cr)
 {
     const std::size_t rows = n.shape[1], cols = n.shape[2];
     const std::size_t ch = n.shape.size() == 4 ? n.shape[3] : 1;
     const std::size_t fe = rows * cols * ch;
-    std::vector<T> in(fe * count);
-    if (!n.mem.empty()) {
-        std::memcpy(in.data(), n.mem.data() + first * fe * sizeof(T), in.size() * sizeof(T));
-    } else {
-        std::fseek(n.f, n.data_off + (long)(first * fe * sizeof(T)), SEEK_SET);
-        if (std::fread(in.data(), sizeof(T), in.size(), n.f) != in.size())
-            throw std::runtime_error("error reading frames");
+    std::vector<T> in(fe);
+    std::vector<T> out(cr.w * cr.h * count);
+    for (std::size_t k = 0; k < count; ++k) {
+        const std::size_t idx = order[first + k];
+        if (!n.mem.empty()) {
+            std::memcpy(in.data(), n.mem.data() + idx * fe * sizeof(T), fe * sizeof(T));
+        } else {
+            std::fseek(n.f, n.data_off + (long)(idx * fe * sizeof(T)), SEEK_SET);
+            if (std::fread(in.data(), sizeof(T), fe, n.f) != fe)
+                throw std::runtime_error("error reading frames");
+        }
+        T* o = out.data() + k * cr.w * cr.h;
+        for (std::size_t y = 0; y < cr.h; ++y)
+            for (std::size_t x = 0; x < cr.w; ++x)
+                o[y * cr.w + x] = in[((cr.t + y) * cols + cr.l + x) * ch + channel];
     }
-    if (ch == 1) {
-        st.push_frames(in.data(), count);
-        return;
-    }
-    std::vector<T> one(rows * cols * count);
-    for (std::size_t i = 0; i < rows * cols * count; ++i)
-        one[i] = in[i * ch + channel];
-    st.push_frames(one.data(), count);
+    st.push_frames(out.data(), count);
 }
 
 } // namespace
@@ -302,6 +322,9 @@ int main(int argc, char* argv[])
     int swSpeckleMasking { 1 };
     int swCalcSum { 1 };
     int swShowVersion { 0 };
+    int swApplyIgnored { 0 };
+    std::size_t ref_frame { 0 };
+    long crop_l = -1, crop_t = -1, crop_w = -1, crop_h = -1;
     std::size_t verbose { 0 };
     try {
         for (int ch = 0; ch != -1;) {
@@ -320,6 +343,7 @@ int main(int argc, char* argv[])
                 { "calcsum", no_argument, &swCalcSum, 1 },
                 { "no-specklemasking", no_argument, &swSpeckleMasking, 0 },
                 { "specklemasking", no_argument, &swSpeckleMasking, 1 },
+                { "apply-ignored", no_argument, &swApplyIgnored, 1 },
                 { 0, 0, 0, 0 }
             };
             int option_index { 0 };
@@ -328,7 +352,7 @@ int main(int argc, char* argv[])
             switch (ch) {
             case 'v': verbose++; break;
             case 'n': max_frames = std::strtoul(optarg, nullptr, 10); break;
-            case 'r': (void)std::strtoul(optarg, nullptr, 10); break; // parsed, unused (main.cpp:132-134)
+            case 'r': ref_frame = std::strtoul(optarg, nullptr, 10); break; // unused by the reference (main.cpp:132-134)
             case 'p': reco_radius = std::strtoul(optarg, nullptr, 10); break;
             case 'b': bispectrum_depth = std::strtoul(optarg, nullptr, 10); break;
             case 'k': {
@@ -338,7 +362,9 @@ int main(int argc, char* argv[])
                 istr >> a >> c >> b;
                 if (a < 0 || b < 0)
                     throw std::range_error("invalid crop box pos arguments");
-                break; // parsed, unused (main.cpp:146-156)
+                crop_l = a;
+                crop_t = b;
+                break; // unused by the reference (main.cpp:146-156)
             }
             case 's': {
                 istr.str(std::string(optarg));
@@ -347,7 +373,9 @@ int main(int argc, char* argv[])
                 istr >> a >> c >> b;
                 if (a <= 0 || b <= 0)
                     throw std::range_error("invalid crop box size arguments");
-                break; // parsed, unused (main.cpp:157-167)
+                crop_w = a;
+                crop_h = b;
+                break; // unused by the reference (main.cpp:157-167)
             }
             case 'c': {
                 const std::string s(optarg);
@@ -377,8 +405,11 @@ int main(int argc, char* argv[])
             usage(progname);
             return 0;
         }
-        (void)swCalcSum;
-        (void)swSpeckleMasking;
+        if (!swApplyIgnored) { // the reference's behaviour: these flags change nothing
+            ref_frame = 0;
+            crop_l = crop_t = crop_w = crop_h = -1;
+            swCalcSum = swSpeckleMasking = 1;
+        }
         const std::string filename(*argv);
 
         Npy npy;
@@ -397,9 +428,33 @@ int main(int argc, char* argv[])
         notice() << "using " << nframes << "/" << npy.shape[0] << " frames\n";
         if (nframes == 0)
             throw std::runtime_error("no frames");
-        const std::size_t rows = npy.shape[1], cols = npy.shape[2];
+        const std::size_t src_rows = npy.shape[1], src_cols = npy.shape[2];
         const std::size_t nch = npy.shape.size() == 4 ? npy.shape[3] : 1;
         const long chan = std::clamp<long>(std::lround(std::log2((double)color_channel)), 0L, (long)nch - 1);
+        Crop cr { 0, 0, src_cols, src_rows };
+        if (crop_l >= 0) {
+            cr.l = (std::size_t)crop_l;
+            cr.t = (std::size_t)crop_t;
+        }
+        if (crop_w > 0) {
+            cr.w = (std::size_t)crop_w;
+            cr.h = (std::size_t)crop_h;
+        } else {
+            cr.w = src_cols > cr.l ? src_cols - cr.l : 0;
+            cr.h = src_rows > cr.t ? src_rows - cr.t : 0;
+        }
+        if (cr.w == 0 || cr.h == 0 || cr.l + cr.w > src_cols || cr.t + cr.h > src_rows)
+            throw std::range_error("crop box outside the frame");
+        if (ref_frame >= nframes)
+            throw std::range_error("reference frame index out of range");
+        // accumulation order: the reference frame first, then the others in order
+        std::vector<std::size_t> order;
+        order.reserve(nframes);
+        order.push_back(ref_frame);
+        for (std::size_t i = 0; i < nframes; ++i)
+            if (i != ref_frame)
+                order.push_back(i);
+        const std::size_t rows = cr.h, cols = cr.w;
 
         info() << "creating bispectrum with size [" << cols << " " << rows << " " << bispectrum_depth << " "
                << bispectrum_depth << "]\n";
@@ -408,30 +463,20 @@ int main(int argc, char* argv[])
         const std::size_t chunk = 256;
         for (std::size_t f0 = 0; f0 < nframes; f0 += chunk) {
             const std::size_t k = std::min(chunk, nframes - f0);
-            if (npy.kind == 'u' && npy.esize == 1) push_chunk<std::uint8_t>(st, npy, f0, k, (std::size_t)chan);
-            else if (npy.kind == 'u') push_chunk<std::uint16_t>(st, npy, f0, k, (std::size_t)chan);
-            else if (npy.esize == 4) push_chunk<float>(st, npy, f0, k, (std::size_t)chan);
-            else push_chunk<double>(st, npy, f0, k, (std::size_t)chan);
+            const std::size_t c = (std::size_t)chan;
+            if (npy.kind == 'u' && npy.esize == 1) push_chunk<std::uint8_t>(st, npy, order, f0, k, c, cr);
+            else if (npy.kind == 'u') push_chunk<std::uint16_t>(st, npy, order, f0, k, c, cr);
+            else if (npy.esize == 4) push_chunk<float>(st, npy, order, f0, k, c, cr);
+            else push_chunk<double>(st, npy, order, f0, k, c, cr);
         }
         if (g_level >= 2) {
             const auto sh = st.shifts();
             for (std::size_t i = 0; i < sh.size(); ++i)
-                std::cerr << "[debug] frame " << i << " relative shift wrt ref frame: [x,y] = [" << sh[i][0] << ","
-                          << sh[i][1] << "]\n";
+                std::cerr << "[debug] frame " << order[i] << " relative shift wrt ref frame: [x,y] = [" << sh[i][0]
+                          << "," << sh[i][1] << "]\n";
         }
-        notice() << "writing bispectrum to file 'bispectrum.dat'\n";
-        st.write_to_file("bispectrum.dat");
-
-        info() << "reconstructing fourier phases from bispectrum\n";
-        const auto res = st.finish((double)reco_radius);
         smip::gpu::Image<double> sum = st.sum();
         smip::gpu::Image<double> power = st.power();
-
-        // main.cpp:329-331: phases windowed by Hann of aperture 2R for the outputs
-        const auto win = smip::gpu::Hann<double>(cols, rows, (double)reco_radius * 2);
-        smip::gpu::Image<std::complex<double>> phases = res.phases;
-        for (std::size_t i = 0; i < phases.size(); ++i)
-            phases.data()[i] *= win.data()[i];
         // main.cpp:359-376: power / (max / 1000); sum / 255
         double pmax = 0.0;
         for (double v : power)
@@ -441,17 +486,33 @@ int main(int argc, char* argv[])
             v /= normfact;
         for (double& v : sum)
             v /= 255.;
+        if (swCalcSum) {
+            save_image("sum_image_falsecolor.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::fabs(sum(x, y)); }, false, true);
+            save_image("sum_image.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::fabs(sum(x, y)); }, false, false);
+        }
+        if (swSpeckleMasking) {
+            notice() << "writing bispectrum to file 'bispectrum.dat'\n";
+            st.write_to_file("bispectrum.dat");
 
-        auto phase01 = [](std::complex<double> z) { return (std::arg(z) + M_PI) / (2 * M_PI); };
-        save_image("sum_image_falsecolor.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::fabs(sum(x, y)); }, false, true);
-        save_image("sum_image.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::fabs(sum(x, y)); }, false, false);
-        save_image("phases_falsecolor.png", cols, rows, [&](std::size_t x, std::size_t y) { return phase01(phases(x, y)); }, true, true);
-        save_image("phases.png", cols, rows, [&](std::size_t x, std::size_t y) { return phase01(phases(x, y)); }, true, false);
-        save_image("phasecons.png", cols, rows, [&](std::size_t x, std::size_t y) { return res.pm.consistency(x, y); }, true, true);
-        save_image("powerspec_falsecolor.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::fabs(power(x, y)); }, true, true);
-        save_image("powerspec.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::fabs(power(x, y)); }, true, false);
-        save_image("reco_image_falsecolor.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::abs(res.image(x, y)); }, true, true);
-        save_image("reco_image.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::abs(res.image(x, y)); }, true, false);
+            info() << "reconstructing fourier phases from bispectrum\n";
+            const auto res = st.finish((double)reco_radius);
+            // main.cpp:329-331: phases windowed by Hann of aperture 2R for the outputs
+            const auto win = smip::gpu::Hann<double>(cols, rows, (double)reco_radius * 2);
+            smip::gpu::Image<std::complex<double>> phases = res.phases;
+            for (std::size_t i = 0; i < phases.size(); ++i)
+                phases.data()[i] *= win.data()[i];
+            auto phase01 = [](std::complex<double> z) { return (std::arg(z) + M_PI) / (2 * M_PI); };
+            save_image("phases_falsecolor.png", cols, rows, [&](std::size_t x, std::size_t y) { return phase01(phases(x, y)); }, true, true);
+            save_image("phases.png", cols, rows, [&](std::size_t x, std::size_t y) { return phase01(phases(x, y)); }, true, false);
+            save_image("phasecons.png", cols, rows, [&](std::size_t x, std::size_t y) { return res.pm.consistency(x, y); }, true, true);
+            save_image("powerspec_falsecolor.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::fabs(power(x, y)); }, true, true);
+            save_image("powerspec.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::fabs(power(x, y)); }, true, false);
+            save_image("reco_image_falsecolor.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::abs(res.image(x, y)); }, true, true);
+            save_image("reco_image.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::abs(res.image(x, y)); }, true, false);
+        } else {
+            save_image("powerspec_falsecolor.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::fabs(power(x, y)); }, true, true);
+            save_image("powerspec.png", cols, rows, [&](std::size_t x, std::size_t y) { return std::fabs(power(x, y)); }, true, false);
+        }
         info() << "done\n";
     } catch (const std::exception& e) {
         std::cerr << "[critical] " << e.what() << "\n";

@@ -71,6 +71,22 @@ def test_cli_rejects_bad_input(tmp_path):
     assert r.returncode == 1 and "crop box" in r.stderr
 
 
+def test_cli_apply_ignored_checks_arguments(tmp_path):
+    """--apply-ignored makes -r, -k and -s take effect; a crop box outside the
+    frame or a reference frame past the last one is an error before any device
+    work (without the switch both are ignored, as in the reference)."""
+    _need_cli()
+    out = subprocess.run([CLI, "-h"], capture_output=True, text=True, check=True)
+    assert "--apply-ignored" in out.stdout
+    src = tmp_path / "s.npy"
+    np.save(src, np.zeros((2, 32, 32), np.uint8))
+    r = subprocess.run([CLI, "--apply-ignored", "-k", "20:0", "-s", "16:16", str(src)], capture_output=True,
+                       text=True, cwd=tmp_path)
+    assert r.returncode == 1 and "crop box outside the frame" in r.stderr
+    r = subprocess.run([CLI, "--apply-ignored", "-r", "2", str(src)], capture_output=True, text=True, cwd=tmp_path)
+    assert r.returncode == 1 and "reference frame index out of range" in r.stderr
+
+
 def _build_api_check(out_dir):
     exe = os.path.join(out_dir, "api_check")
     cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I" + os.path.join(ROOT, "include"),
@@ -179,3 +195,42 @@ def test_cli_reads_animated_gif(smip, tmp_path):
             assert r.returncode == 0, r.stderr
         assert open(d_gif / "bispectrum.dat", "rb").read() == open(d_npy / "bispectrum.dat", "rb").read()
         assert np.array_equal(read_png16(d_gif / "sum_image.png"), read_png16(d_npy / "sum_image.png"))
+
+
+@pytest.mark.gpu
+def test_cli_apply_ignored(smip, tmp_path):
+    """--apply-ignored -r 3 -k 32:16 -s 64:64: frame 3 is the correlation
+    reference and every frame is cut to the 64x64 box at column 32, row 16;
+    --no-calcsum drops the sum images, --no-specklemasking the bispectrum and
+    everything made from it.  Outputs equal the binding on those frames."""
+    _need_cli()
+    from smip_gb300 import synthetic as S
+
+    frames = S.make_stack(S.config_spec("binary128", nframes=12))
+    src = tmp_path / "stack.npy"
+    np.save(src, frames)
+    d1, d2 = tmp_path / "a", tmp_path / "b"
+    d1.mkdir()
+    d2.mkdir()
+    base = [CLI, "--apply-ignored", "-r", "3", "-k", "32:16", "-s", "64:64", "-b", "16", "-p", "20"]
+    r = subprocess.run(base + ["--no-calcsum", str(src)], capture_output=True, text=True, cwd=d1)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run(base + ["--no-specklemasking", str(src)], capture_output=True, text=True, cwd=d2)
+    assert r.returncode == 0, r.stderr
+    order = [3] + [i for i in range(12) if i != 3]
+    used = np.ascontiguousarray(frames[order][:, 16:80, 32:96])
+    with smip.Stack(64, 64, 16) as st:
+        st.push_frames(used)
+        ref_dat = tmp_path / "ref.dat"
+        st.save_bispectrum(str(ref_dat))
+        img, _, _, _ = st.finish(20.0)
+        sm = st.sum()
+    assert open(d1 / "bispectrum.dat", "rb").read() == open(ref_dat, "rb").read()
+    assert not (d1 / "sum_image.png").exists() and not (d1 / "sum_image_falsecolor.png").exists()
+    exp = np.clip(np.roll(np.abs(img), (32, 32), axis=(0, 1)) * 65535.0, 0, 65535).astype(np.uint16)
+    assert np.abs(read_png16(d1 / "reco_image.png").astype(np.int64) - exp).max() <= 1
+    for name in ("bispectrum.dat", "reco_image.png", "phases.png", "phasecons.png"):
+        assert not (d2 / name).exists(), name
+    exp = np.clip(np.abs(sm / 255.0) * 65535.0, 0, 65535).astype(np.uint16)
+    assert np.abs(read_png16(d2 / "sum_image.png").astype(np.int64) - exp).max() <= 1
+    assert read_png16(d2 / "powerspec.png").shape == (64, 64)

@@ -250,7 +250,8 @@ def test_reference_example_matches_published_images(gif_check, oracle, tmp_path)
     if not os.path.exists(os.path.join(d, "hu940ani.gif")):
         pytest.skip("reference data not present")
     frames = decode(gif_check, os.path.join(d, "hu940ani.gif"), tmp_path)
-    red = np.ascontiguousarray(frames[..., 2])  # -c r: channel 4 -> index 2 of B, G, R
+    # -c r: channel round(log2(1)) = 0 of B, G, R (videoio.h:78-79); B equals R in this GIF
+    red = np.ascontiguousarray(frames[..., 0])
     n, H, W = red.shape
     out = oracle.run_stack(red, 32, 64)
 
