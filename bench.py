@@ -74,7 +74,9 @@ def gen_frames(spec, nframes, procs):
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks/throttle reasons sampled every 50 ms.  Entering waits
+    (at most 3 s) for the first sample, so that sampling runs before the timed
+    region starts."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -94,6 +96,11 @@ class ClockSampler:
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+        t0 = time.time()
+        while self.proc and self.proc.poll() is None and time.time() - t0 < 3.0:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.01)
         return self
 
     def __exit__(self, *exc):
@@ -451,7 +458,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD, choices=[WORKLOAD, "binary128", "extended512"])

@@ -127,6 +127,29 @@ def test_accumulate_fft_shapes(smip, oracle, W, H, D):
     assert np.all(got[B64 == 0] == 0)
 
 
+@pytest.mark.parametrize("W,H,D,n", [(64, 64, 16, 40), (128, 64, 40, 9), (256, 256, 32, 20), (512, 512, 48, 16)])
+def test_every_element_accumulated_once(smip, oracle, W, H, D, n):
+    """Write-count check of the bispectrum kernel: with every spectrum value
+    1 + 0i each in-range triple adds exactly 1 per frame, so the normalised
+    bispectrum holds, per packed element, how many times the kernel
+    accumulated it -- 1 where the reference's loop (bispectrum.h:393-408)
+    writes and 0 elsewhere, exactly.  A tile computed twice, a split part
+    merged twice or lost, or a stage read while being refilled shows up as a
+    value other than 0 or 1.  At 64x64 with 40 frames (37 tiles, 4 parts each)
+    and 512x512 with 16 frames (the last wave's 16 tiles, 2 parts each) tiles
+    are split by frames, so the merge of the parts is covered too."""
+    ones = np.ones((H, W), np.complex128)
+    d = bispec_desc(W, H, D)
+    cnt = np.zeros(d["base_size"], np.complex64)  # 0 and 1 are exact in FP32
+    oracle.accumulate(cnt, ones, D)
+    assert set(np.unique(cnt.real)) <= {0.0, 1.0} and np.all(cnt.imag == 0)
+    with smip.Stack(W, H, D) as st:
+        st.accumulate_from_fft(np.broadcast_to(ones, (n, H, W)))
+        got = st.bispectrum()
+    assert np.array_equal(got.real, cnt.real)
+    assert np.all(got.imag == 0)
+
+
 @pytest.mark.parametrize("key", ["n16_d4", "n24_d6", "n32_d8"])
 def test_device_get_element_index(smip, key):
     """The device copy of get_element's index path is bit-identical to the
