@@ -1,7 +1,7 @@
 """GPU parity: libsmip_gpu.so (through its C ABI) against the reference's
 fixtures and the CPU oracle on the same seeded frames.
 
-Tolerances (spec: SAA shifts bit-exact, phases within 1e-3 rad of FP64):
+Tolerances (targets: SAA shifts bit-exact, phases within 1e-3 rad of FP64):
   shifts, shift-and-add sum, phase-map flags ............ bit-exact
   power spectrum ........ max |dP| <= 1e-6 max P, rel-L2 <= 1e-6
   bispectrum (normalised) rel-L2 <= 1e-5 against the FP64 oracle
