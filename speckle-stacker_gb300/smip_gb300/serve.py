@@ -13,7 +13,11 @@ many jobs share one device:
   whose frames are all in to a worker thread for phase recovery and the final
   image, while the loop keeps feeding the others;
 * stacks are pooled by shape and reset between jobs, so the loop allocates no
-  device memory after warm-up.
+  device memory after warm-up;
+* a job fails alone: an error while its frames are pushed or while it is
+  reconstructed, a producer that delivers no frames for ``stall_timeout``
+  seconds, or ``Engine.cancel`` gives that job a result with ``error`` set
+  and its bytes back to the budget, while the other jobs go on.
 
 ``run_plain`` is the single-job path (one job at a time, in arrival order)
 that the served numbers are compared with.  A job's results do not depend on
@@ -23,6 +27,7 @@ mix, so results are identical, which ``tests/test_serve.py`` checks.
 from __future__ import annotations
 
 import concurrent.futures as cf
+import threading
 import time
 from dataclasses import dataclass, field
 from typing import Callable, Dict, List, Optional, Tuple
@@ -70,6 +75,13 @@ class Job:
     def shape(self) -> Tuple[int, int, int]:
         return (self.frames.shape[2], self.frames.shape[1], self.bdepth)
 
+    def available(self) -> int:
+        """Frames the producer has delivered so far: a frame source with an
+        ``available()`` method (frames still arriving) reports it, an array
+        or FrameRing holds all of them."""
+        f = getattr(self.frames, "available", None)
+        return int(f()) if callable(f) else len(self.frames)
+
     def parts(self, pos: int, k: int):
         if isinstance(self.frames, FrameRing):
             return self.frames.parts(pos, k)
@@ -83,11 +95,12 @@ class JobResult:
     arrival: float
     admitted: float
     done: float
-    image: np.ndarray = field(repr=False)
-    phases: np.ndarray = field(repr=False)
-    flags: np.ndarray = field(repr=False)
-    consistency: np.ndarray = field(repr=False)
-    shifts: np.ndarray = field(repr=False)
+    image: Optional[np.ndarray] = field(repr=False)
+    phases: Optional[np.ndarray] = field(repr=False)
+    flags: Optional[np.ndarray] = field(repr=False)
+    consistency: Optional[np.ndarray] = field(repr=False)
+    shifts: Optional[np.ndarray] = field(repr=False)
+    error: Optional[str] = None  # set (arrays None) when the job failed or was cancelled
 
     @property
     def latency(self) -> float:
@@ -103,10 +116,16 @@ def bispectrum_bytes(ncols: int, nrows: int, bdepth: int) -> int:
 
 
 def summarize(results: List[JobResult], makespan: float) -> dict:
-    lat = np.array([r.latency for r in results]) * 1e3
-    frames = sum(r.nframes for r in results)
-    return {"jobs": len(results), "frames": frames, "seconds": makespan, "frames_per_s": frames / makespan,
-            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
+    """Throughput and latency of the jobs that completed; failed or cancelled
+    jobs are counted apart."""
+    ok = [r for r in results if r.error is None]
+    lat = np.array([r.latency for r in ok] or [0.0]) * 1e3
+    frames = sum(r.nframes for r in ok)
+    out = {"jobs": len(ok), "frames": frames, "seconds": makespan, "frames_per_s": frames / makespan,
+           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
+    if len(ok) != len(results):
+        out["failed"] = len(results) - len(ok)
+    return out
 
 
 class Engine:
@@ -119,11 +138,13 @@ class Engine:
     graph: the last batches of the jobs whose frames are all in after a round
         run as one CUDA graph launch (smip_gb300.batch_launch) before their
         reconstructions start, instead of one flush per job.
+    stall_timeout: seconds a streaming job may go without new frames from its
+        producer before it fails (None: wait for ever).
     """
 
     def __init__(self, device: int = 0, budget_bytes: float = 120e9, max_active: int = 64, workers: int = 32,
                  stack_factory: Optional[Callable] = None, graph: bool = False,
-                 batch_launch: Optional[Callable] = None):
+                 batch_launch: Optional[Callable] = None, stall_timeout: Optional[float] = None):
         if stack_factory is None:
             from smip_gb300 import Stack
 
@@ -137,9 +158,24 @@ class Engine:
         self.budget = float(budget_bytes)
         self.max_active = int(max_active)
         self.workers = int(workers)
+        self.stall_timeout = stall_timeout
         self.pool: Dict[Tuple[int, int, int], list] = {}
         self.peak_bytes = 0.0
         self.peak_active = 0
+        self._cancel_lock = threading.Lock()
+        self._cancelled: set = set()
+
+    def cancel(self, job_id: int):
+        """Cancels a job that is waiting or still streaming (callable from any
+        thread while ``run`` serves).  It ends with error "cancelled" and its
+        stack goes back to the pool; a job already being reconstructed
+        completes normally."""
+        with self._cancel_lock:
+            self._cancelled.add(job_id)
+
+    def _is_cancelled(self, job_id: int) -> bool:
+        with self._cancel_lock:
+            return job_id in self._cancelled
 
     def prewarm(self, shapes, count: int = 1):
         """Creates ``count`` pooled stacks per (ncols, nrows, bdepth) shape, so
@@ -154,8 +190,12 @@ class Engine:
         return lst.pop() if lst else self.factory(*shape)
 
     def _release(self, shape, st):
-        st.reset()
-        self.pool[shape].append(st)
+        try:
+            st.reset()
+        except Exception:  # a stack that cannot be reset is not reused
+            self._discard(st)
+            return
+        self.pool.setdefault(shape, []).append(st)
 
     @staticmethod
     def _finish(job: Job, st, t0: float, admitted: float) -> JobResult:
@@ -163,19 +203,37 @@ class Engine:
         sh = st.shifts()
         return JobResult(job.id, len(job.frames), job.arrival, admitted, time.perf_counter() - t0, img, ph, fl, cs, sh)
 
+    @staticmethod
+    def _failed(job: Job, t0: float, admitted: float, nframes: int, why: str) -> JobResult:
+        return JobResult(job.id, nframes, job.arrival, admitted, time.perf_counter() - t0, None, None, None, None,
+                         None, error=why)
+
+    @staticmethod
+    def _discard(st):
+        """A stack whose job failed on a device call is not reused."""
+        close = getattr(st, "close", None)
+        if callable(close):
+            try:
+                close()
+            except Exception:  # the failure is already reported for the job
+                pass
+
     def run(self, jobs: List[Job], realtime: bool = True) -> Tuple[List[JobResult], float]:
         """Serves ``jobs``; with ``realtime`` a job is only visible from its
         arrival time on, otherwise all are queued at once (batched mode).
         Returns (results in completion order, makespan in seconds)."""
         waiting = sorted(jobs, key=lambda j: (j.arrival, j.id))
-        active: list = []          # [job, stack, frames pushed, admitted time, bytes]
-        running: dict = {}         # future -> (job, stack, bytes)
+        active: list = []          # [job, stack, frames pushed, admitted time, bytes, time of last frames]
+        running: dict = {}         # future -> (job, stack, bytes, admitted time)
         results: List[JobResult] = []
         used = 0.0
         t0 = time.perf_counter()
         with cf.ThreadPoolExecutor(max_workers=self.workers) as ex:
             while waiting or active or running:
                 now = time.perf_counter() - t0
+                for job in [j for j in waiting if self._is_cancelled(j.id)]:
+                    waiting.remove(job)
+                    results.append(self._failed(job, t0, now, 0, "cancelled"))
                 # admission: FIFO, by slots and bispectrum bytes
                 while waiting and (not realtime or waiting[0].arrival <= now) \
                         and len(active) + len(running) < self.max_active:
@@ -185,7 +243,7 @@ class Engine:
                         break
                     waiting.pop(0)
                     used += need
-                    active.append([job, self._acquire(job.shape), 0, now, need])
+                    active.append([job, self._acquire(job.shape), 0, now, need, now])
                 self.peak_bytes = max(self.peak_bytes, used)
                 self.peak_active = max(self.peak_active, len(active) + len(running))
                 # one chunk per streaming job, round robin
@@ -193,29 +251,56 @@ class Engine:
                 ready = []
                 for entry in list(active):
                     job, st, pos = entry[0], entry[1], entry[2]
-                    k = min(job.chunk, len(job.frames) - pos)
-                    for part in job.parts(pos, k):
-                        st.push_frames(part)
-                    entry[2] = pos + k
-                    pushed = True
-                    if entry[2] == len(job.frames):
+                    why = None
+                    if self._is_cancelled(job.id):
+                        why = "cancelled"
+                    else:
+                        k = min(job.chunk, job.available() - pos, len(job.frames) - pos)
+                        if k > 0:
+                            try:
+                                for part in job.parts(pos, k):
+                                    st.push_frames(part)
+                            except Exception as e:  # this job's frames or device call failed
+                                active.remove(entry)
+                                used -= entry[4]
+                                self._discard(st)
+                                results.append(self._failed(job, t0, entry[3], pos, f"push failed: {e}"))
+                                continue
+                            entry[2] = pos + k
+                            entry[5] = now
+                            pushed = True
+                        elif self.stall_timeout is not None and now - entry[5] > self.stall_timeout:
+                            why = f"producer stalled: no frames for {self.stall_timeout:g} s after frame {pos}"
+                    if why is not None:
+                        active.remove(entry)
+                        used -= entry[4]
+                        self._release(job.shape, st)
+                        results.append(self._failed(job, t0, entry[3], entry[2], why))
+                    elif entry[2] == len(job.frames):
                         active.remove(entry)
                         ready.append(entry)
                 if self.graph and ready:
                     self.batch_launch([e[1] for e in ready])
                 for entry in ready:
                     fut = ex.submit(self._finish, entry[0], entry[1], t0, entry[3])
-                    running[fut] = (entry[0], entry[1], entry[4])
+                    running[fut] = (entry[0], entry[1], entry[4], entry[3])
                 # completions
                 done = [f for f in running if f.done()]
                 for f in done:
-                    job, st, need = running.pop(f)
-                    results.append(f.result())
-                    self._release(job.shape, st)
+                    job, st, need, admitted = running.pop(f)
                     used -= need
+                    try:
+                        results.append(f.result())
+                    except Exception as e:  # reconstruction failed: report it, drop the stack
+                        self._discard(st)
+                        results.append(self._failed(job, t0, admitted, len(job.frames), f"finish failed: {e}"))
+                        continue
+                    self._release(job.shape, st)
                 if not pushed and not done:
                     if running:
                         cf.wait(list(running), timeout=0.002, return_when=cf.FIRST_COMPLETED)
+                    elif active:
+                        time.sleep(0.001)  # every streaming job waits for its producer
                     elif waiting:
                         time.sleep(max(0.0, min(0.002, waiting[0].arrival - (time.perf_counter() - t0))))
         return results, time.perf_counter() - t0

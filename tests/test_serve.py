@@ -200,3 +200,95 @@ def test_batch_launch_matches_flush(smip):
     with smip.Stack(64, 64, 16) as st, pytest.raises(smip.InvalidArgument):
         st.push_frames(frames[0][:3])
         smip.batch_launch([st, st])
+
+
+class FailingStack(FakeStack):
+    """FakeStack whose push fails on a frame holding 255 and whose finish
+    fails for a negative reco radius, as a device or shape error would."""
+
+    def push_frames(self, f):
+        if np.any(np.asarray(f) == 255):
+            raise RuntimeError("injected device error")
+        super().push_frames(f)
+
+    def finish(self, R):
+        if R < 0:
+            raise RuntimeError("injected reconstruction error")
+        return super().finish(R)
+
+
+class Producer:
+    """Frames delivered by a producer thread: ``available()`` frames so far;
+    ``stop_at`` freezes it there (a stalled producer)."""
+
+    def __init__(self, frames, stop_at):
+        self.frames, self.stop_at = frames, stop_at
+        self.shape = frames.shape
+
+    def __len__(self):
+        return len(self.frames)
+
+    def __getitem__(self, s):
+        return self.frames[s]
+
+    def available(self):
+        return min(self.stop_at, len(self.frames))
+
+
+def test_engine_isolates_failing_jobs():
+    """A job whose push fails and one whose reconstruction fails end with an
+    error; every other job completes with the result it has alone."""
+    jobs = _jobs(14)
+    jobs[3].frames = jobs[3].frames.copy()
+    jobs[3].frames[len(jobs[3].frames) // 2, 0, 0] = 255  # fails in the middle of its frames
+    jobs[7].reco_radius = -1.0
+    eng = serve.Engine(max_active=4, workers=2, stack_factory=FailingStack)
+    res, span = eng.run(jobs, realtime=False)
+    by_id = {r.id: r for r in res}
+    assert sorted(by_id) == list(range(14))
+    assert by_id[3].error.startswith("push failed") and by_id[3].image is None
+    assert by_id[7].error.startswith("finish failed") and by_id[7].nframes == len(jobs[7].frames)
+    ok = [j for j in jobs if j.id not in (3, 7)]
+    plain, _ = serve.run_plain(ok, realtime=False, stack_factory=FakeStack)
+    for r in plain:
+        assert by_id[r.id].error is None and np.array_equal(by_id[r.id].image, r.image)
+    s = serve.summarize(res, span)
+    assert s["jobs"] == 12 and s["failed"] == 2
+
+
+def test_engine_stalled_producer_times_out():
+    """A producer that stops after 16 of 40 frames fails its job after
+    stall_timeout; the other jobs are served meanwhile."""
+    jobs = _jobs(6)
+    fr = np.random.default_rng(9).integers(0, 200, (40, 16, 16)).astype(np.uint8)
+    jobs.append(serve.Job(99, Producer(fr, 16), 8, 6.0, chunk=8))
+    eng = serve.Engine(max_active=8, workers=2, stack_factory=FakeStack, stall_timeout=0.05)
+    res, _ = eng.run(jobs, realtime=False)
+    by_id = {r.id: r for r in res}
+    assert by_id[99].error.startswith("producer stalled") and by_id[99].nframes == 16
+    assert all(by_id[j.id].error is None for j in jobs[:6])
+
+
+def test_engine_cancel_while_streaming_and_waiting():
+    """cancel() from another thread ends a job whose producer is stuck, and a
+    job still waiting for admission; both report "cancelled"."""
+    import threading
+
+    jobs = _jobs(4)
+    fr = np.random.default_rng(10).integers(0, 200, (40, 16, 16)).astype(np.uint8)
+    jobs.append(serve.Job(50, Producer(fr, 8), 8, 6.0, chunk=8))     # never completes by itself
+    jobs.append(serve.Job(51, fr, 8, 6.0, arrival=30.0, chunk=8))    # arrives far in the future
+    eng = serve.Engine(max_active=8, workers=2, stack_factory=FakeStack)
+
+    def stop():
+        eng.cancel(50)
+        eng.cancel(51)
+
+    threading.Timer(0.05, stop).start()
+    t = __import__("time").perf_counter()
+    res, _ = eng.run(jobs, realtime=True)
+    assert __import__("time").perf_counter() - t < 10.0
+    by_id = {r.id: r for r in res}
+    assert by_id[50].error == "cancelled" and by_id[50].nframes == 8
+    assert by_id[51].error == "cancelled" and by_id[51].nframes == 0
+    assert all(by_id[j.id].error is None for j in jobs[:4])
