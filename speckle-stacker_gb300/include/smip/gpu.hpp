@@ -233,6 +233,16 @@ public:
         check(smip_stack_load_bispectrum(handle(), path.c_str(), nframes));
     }
     void merge(const Stack& src) { check(smip_stack_merge(handle(), src.handle())); }
+    // src correlates against this stack's reference frame (before src's first frame; then merge(src))
+    void share_reference(Stack& src) const { check(smip_stack_share_reference(handle(), src.handle())); }
+    // the bispectrum.dat payload from memory (base_size normalised elements) into an empty stack
+    void set_bispectrum(const std::vector<std::complex<float>>& b, long nframes = 0)
+    {
+        check(smip_stack_set_bispectrum(handle(), reinterpret_cast<const float*>(b.data()), nframes));
+    }
+    // whole-stack checkpoint: every accumulator, the frame count, shifts and reference frame
+    void save_state(const std::string& path) const { check(smip_stack_save_state(handle(), path.c_str())); }
+    void load_state(const std::string& path) { check(smip_stack_load_state(handle(), path.c_str())); }
 
 protected:
     void check_shape(std::size_t nx, std::size_t ny) const
