@@ -230,6 +230,13 @@ SMIP_GPU_API int smip_xcorr_displacement(int device, const double* ref, const do
 SMIP_GPU_API int smip_xcorr_displacement_noalloc(const double* ref, const double* frame, long ncols, long nrows,
                                                  int* shift, void* stream);
 
+/* Array2<double>::shifted(DimVector<int,2>{dx, dy}) (array2.h:603-622) on the
+ * GPU: out(x, y) = in(x - dx, y - dy), zero where that lies outside; ncols x
+ * nrows doubles, row-major, host memory.  |dx| >= ncols or |dy| >= nrows is
+ * SMIP_E_OUT_OF_RANGE: the reference's clamped copy range reads outside the
+ * array there.  The stack pipeline fuses this shift into its shift-and-add. */
+SMIP_GPU_API int smip_shifted(int device, const double* in, double* out, long ncols, long nrows, int dx, int dy);
+
 /* Hann<double>(xsize, ysize, aperture) (window_function.h:39-46, 70-85),
  * computed on the GPU; SMIP_E_DOMAIN for aperture <= 0. */
 SMIP_GPU_API int smip_hann(int device, double* out, long xsize, long ysize, double aperture);

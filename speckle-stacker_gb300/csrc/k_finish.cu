@@ -143,6 +143,26 @@ cudaError_t launch_power_full(const double* Phalf, double pnorm, const Geometry&
     return cudaGetLastError();
 }
 
+// Array2<double>::shifted(distance) (array2.h:603-622): element (x, y) of the
+// result is in(x - dx, y - dy), zero where that lies outside.  For |dx| < W and
+// |dy| < H this is exactly the reference's clamped copy range.
+__global__ void shifted_kernel(const double* __restrict__ in, double* __restrict__ out, int W, int H, int dx, int dy)
+{
+    const int n = W * H;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int x = i % W, y = i / W;
+        const int sx = x - dx, sy = y - dy;
+        out[i] = (sx >= 0 && sx < W && sy >= 0 && sy < H) ? in[sx + sy * W] : 0.0;
+    }
+}
+
+cudaError_t launch_shifted(const double* in, double* out, int W, int H, int dx, int dy, cudaStream_t st)
+{
+    const int n = W * H;
+    shifted_kernel<<<grid_n(n), 256, 0, st>>>(in, out, W, H, dx, dy); note_launches(1);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_hann(double* out, int W, int H, double aperture, cudaStream_t st)
 {
     const int n = W * H;

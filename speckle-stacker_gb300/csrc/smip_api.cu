@@ -1575,6 +1575,34 @@ extern "C" int smip_bispec_offsets(int device, long ncols, long nrows, long bdep
     return SMIP_OK;
 }
 
+extern "C" int smip_shifted(int device, const double* in, double* out, long ncols, long nrows, int dx, int dy)
+{
+    if (!in || !out)
+        return fail(SMIP_E_INVALID_ARGUMENT, "null array");
+    if (ncols <= 0 || nrows <= 0 || ncols * nrows > (1L << 30))
+        return fail(SMIP_E_INVALID_ARGUMENT, "invalid array size");
+    // the reference's clamped range reads outside the array for |distance| >= size
+    if (dx <= -ncols || dx >= ncols || dy <= -nrows || dy >= nrows)
+        return fail(SMIP_E_OUT_OF_RANGE, "Array2::shifted: distance not smaller than the array size");
+    CUDA_TRY(cudaSetDevice(device));
+    const size_t bytes = sizeof(double) * (size_t)(ncols * nrows);
+    double *din = nullptr, *dout = nullptr;
+    CUDA_TRY(cudaMalloc(&din, bytes));
+    cudaError_t e = cudaMalloc(&dout, bytes);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(din, in, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = launch_shifted(din, dout, (int)ncols, (int)nrows, dx, dy, 0);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(out, dout, bytes, cudaMemcpyDeviceToHost);
+    cudaFree(din);
+    if (dout)
+        cudaFree(dout);
+    if (e != cudaSuccess)
+        return fail(SMIP_E_CUDA, cudaGetErrorString(e));
+    return SMIP_OK;
+}
+
 extern "C" int smip_hann(int device, double* out, long xsize, long ysize, double aperture)
 {
     if (!out)

@@ -137,6 +137,8 @@ cudaError_t launch_finish(const double* Phalf, double pnorm, const double2* phas
 cudaError_t launch_power_full(const double* Phalf, double pnorm, const Geometry& g, double* power_full,
                               cudaStream_t st);
 cudaError_t launch_hann(double* out, int W, int H, double aperture, cudaStream_t st);
+// Array2<double>::shifted: out(x, y) = in(x - dx, y - dy), zero outside.
+cudaError_t launch_shifted(const double* in, double* out, int W, int H, int dx, int dy, cudaStream_t st);
 
 // Sum of squares of a frame (double), for the correlation error bound.
 cudaError_t launch_sumsq(int dtype, const void* frame, long long n, double* out, cudaStream_t st);

@@ -379,6 +379,16 @@ private:
     bool m_ready = false;
 };
 
+// Array2<T>::shifted(distance) (array2.h:603-622), on the GPU in double:
+// element (x, y) of the result is a(x - dx, y - dy), zero outside.
+template <class T> Image<double> shifted(const Image<T>& a, std::array<int, 2> distance, int device = 0)
+{
+    std::vector<double> in(a.begin(), a.end());
+    Image<double> out(a.ncols(), a.nrows());
+    check(smip_shifted(device, in.data(), out.data(), (long)a.ncols(), (long)a.nrows(), distance[0], distance[1]));
+    return out;
+}
+
 // Hann<T>(xsize, ysize, aperture) (window_function.h:39-46, 70-85)
 template <class T = double> Image<T> Hann(std::size_t xsize, std::size_t ysize, double aperture, int device = 0)
 {

@@ -116,6 +116,7 @@ def _load():
         "smip_reco_visits": ([C.c_double, ip, C.c_long, lp], C.c_int),
         "smip_xcorr_displacement": ([C.c_int, dp, dp, C.c_long, C.c_long, ip, ip, dp], C.c_int),
         "smip_hann": ([C.c_int, dp, C.c_long, C.c_long, C.c_double], C.c_int),
+        "smip_shifted": ([C.c_int, dp, dp, C.c_long, C.c_long, C.c_int, C.c_int], C.c_int),
         "smip_bispec_offsets": ([C.c_int, C.c_long, C.c_long, C.c_long, ip, C.c_long,
                                  C.POINTER(C.c_longlong), ip], C.c_int),
         "smip_xcorr_displacement_noalloc": ([vp, vp, C.c_long, C.c_long, vp, vp], C.c_int),
@@ -418,6 +419,16 @@ def hann(xsize: int, ysize: int, aperture: float, device: int = 0):
     """Hann<double>(xsize, ysize, aperture) as an Array2 in FFT order (ysize, xsize)."""
     out = np.zeros((ysize, xsize), np.float64)
     _check(_L().smip_hann(device, _p(out, C.c_double), xsize, ysize, float(aperture)))
+    return out
+
+
+def shifted(a, dx: int, dy: int, device: int = 0):
+    """Array2<double>::shifted({dx, dy}) (array2.h:603-622) on the GPU: the
+    (nrows, ncols) array moved by (dx, dy), zero-filled; OutOfRange for a
+    distance not smaller than the array."""
+    a = np.ascontiguousarray(a, np.float64)
+    out = np.zeros_like(a)
+    _check(_L().smip_shifted(device, _p(a, C.c_double), _p(out, C.c_double), a.shape[1], a.shape[0], int(dx), int(dy)))
     return out
 
 

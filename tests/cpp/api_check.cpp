@@ -113,6 +113,8 @@ int main(int argc, char** argv)
     g::NextRecoIndex(r, phi, i, j);
     const int rij[2] = { i, j };
     dump(dir + "/next_reco.bin", rij, 2);
+    const auto shf = g::shifted(frames[0], { 3, -2 });
+    dump(dir + "/shifted.bin", shf.data(), shf.size());
     const auto w = g::Hann<double>(N, N, 48.0);
     dump(dir + "/hann.bin", w.data(), w.size());
     std::cout << "ok\n";

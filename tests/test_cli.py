@@ -169,6 +169,7 @@ def test_cpp_layer_matches_binding(smip, tmp_path):
     assert np.array_equal(np.fromfile(tmp_path / "stack_flags.bin", np.uint8), fl.ravel())
     assert tuple(np.fromfile(tmp_path / "next_reco.bin", np.int32)) == smip.next_reco_index(0.0, 0.0, 0, 0)[2:]
     assert np.array_equal(np.fromfile(tmp_path / "hann.bin", np.float64), smip.hann(64, 64, 48.0).ravel())
+    assert np.array_equal(np.fromfile(tmp_path / "shifted.bin", np.float64), smip.shifted(frames[0], 3, -2).ravel())
 
 
 @pytest.mark.gpu

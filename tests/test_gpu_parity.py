@@ -283,6 +283,20 @@ def test_standalone_reconstruct_phases(smip, oracle):
     assert np.abs(cs - fx["consistency"]).max() <= 1e-5
 
 
+def test_shifted_matches_oracle(smip, oracle):
+    """Array2<double>::shifted for shifts inside the array, edges included,
+    against the oracle's restatement of array2.h:603-622; a distance as large
+    as the array (where the reference reads outside it) is OutOfRange."""
+    rng = np.random.default_rng(11)
+    a = rng.normal(size=(32, 64))
+    for dx, dy in [(0, 0), (3, -5), (-17, 9), (63, 31), (-63, -31), (1, 0), (0, -1)]:
+        assert np.array_equal(smip.shifted(a, dx, dy), oracle.shifted(a, dx, dy)), (dx, dy)
+    with pytest.raises(smip.OutOfRange):
+        smip.shifted(a, 64, 0)
+    with pytest.raises(smip.OutOfRange):
+        smip.shifted(a, 0, -32)
+
+
 def test_hann_matches_reference_formula(smip, oracle):
     assert np.abs(smip.hann(64, 32, 48.0) - oracle.hann(64, 32, 48.0)).max() <= 1e-15
 
