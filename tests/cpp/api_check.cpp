@@ -69,17 +69,21 @@ int main(int argc, char** argv)
         if (p1.data()[i] != p2.data()[i])
             return 4;
     // whole-stack checkpoint: 3 frames, save, load into a new stack, 3 more
-    // frames -> the same bispectrum as the 6-frame stack above
+    // frames -> the bispectrum of one stack that takes all 6 (3-frame
+    // batches, so that both sum the same frames per batch)
     {
-        g::Stack a(N, N, 20);
+        g::Stack u(N, N, 20, 0, nullptr, 3);
+        for (int f = 0; f < 6; ++f)
+            u.push_frame(frames[f]);
+        g::Stack a(N, N, 20, 0, nullptr, 3);
         for (int f = 0; f < 3; ++f)
             a.push_frame(frames[f]);
         a.save_state(dir + "/state.bin");
-        g::Stack c(N, N, 20);
+        g::Stack c(N, N, 20, 0, nullptr, 3);
         c.load_state(dir + "/state.bin");
         for (int f = 3; f < 6; ++f)
             c.push_frame(frames[f]);
-        if (c.bispectrum() != b)
+        if (c.bispectrum() != u.bispectrum())
             return 7;
         // the bispectrum from memory reconstructs as the original stack does
         g::Stack m(N, N, 20);
