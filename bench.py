@@ -187,6 +187,41 @@ def cpu_baseline(frames, depth, budget_s=12.0, threads=None):
                       f"bispectrum d={depth}), {el:.1f} s"}
 
 
+def accuracy_check(G, spec, device, nframes=16, threads=None):
+    """The oracle as the checker: the first ``nframes`` frames of the workload
+    through the GPU stack and through the FP64 oracle (same seeded frames,
+    the workload's depth and reco radius); the errors the parity tests bound."""
+    from oracle import Oracle
+
+    from smip_gb300 import synthetic as S
+
+    threads = threads or os.cpu_count() or 1
+    sample = S.make_stack(spec, 0, nframes)
+    R = float(spec.reco_radius)
+    exp = Oracle().run_stack(sample, spec.bdepth, R, fp64=True, nthreads=threads)
+    n = sample.shape[1]
+    with G.Stack(n, n, spec.bdepth, device=device, batch_frames=8) as st:
+        st.push_frames(sample)
+        sh, sm, pw, bs = st.shifts(), st.sum(), st.power(), st.bispectrum()
+        img, ph, fl, _ = st.finish(R)
+
+    def rel(a, b):
+        a, b = np.asarray(a, np.complex128).ravel(), np.asarray(b, np.complex128).ravel()
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    m = exp["flags"] > 0
+    d = np.abs(np.angle(ph[m] * np.conj(exp["phases"][m])))
+    p_exp = np.real(exp["power"])
+    return {"frames": nframes, "against": "FP64 oracle (C restatement of the reference, pinned to its build)",
+            "shifts_bit_exact": bool(np.array_equal(sh, exp["shifts"])),
+            "sum_bit_exact": bool(np.array_equal(sm.view(np.uint64), np.asarray(exp["sum"]).view(np.uint64))),
+            "flags_identical": bool(np.array_equal(fl, exp["flags"])),
+            "phase_max_rad": float(d.max()) if d.size else 0.0,
+            "phase_rms_rad": float(np.sqrt((d ** 2).mean())) if d.size else 0.0,
+            "power_max_rel": float(np.abs(pw - p_exp).max() / p_exp.max()),
+            "bispectrum_rel_l2": rel(bs, exp["bispec"]), "image_rel_l2": rel(img, exp["image"])}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -430,6 +465,7 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(frames, D)
+        cpu["check"] = accuracy_check(G, spec, local, nframes=16 if n <= 256 else 4)
     serving = serving_metrics(serve_jobs) if serve_jobs else None
     line = {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
