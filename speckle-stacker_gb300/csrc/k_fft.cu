@@ -47,9 +47,13 @@ __device__ __forceinline__ float2 df_round(const dfc& v) { return make_float2(v.
 // Two real rows per complex FFT of length W (x0 + i x1), float-float; the
 // half-spectra are separated afterwards.  Output G'(a, y) = sum_x f(x, y)
 // exp(+2 pi i a x / W), float-float, stored [f][a][y].
+// copy_out (optional): the frames as read, written to device memory [f][y][x]
+// with the same stride -- the batch's frame buffer when the frames are read
+// straight from mapped page-locked host memory.
 template <typename T>
 __global__ void __launch_bounds__(256, 4) row_pass_kernel(const T* __restrict__ frames, long long fstride, int logW, int H,
-                                                        int hw, dfc* __restrict__ Gt, const dfc* __restrict__ tw_g)
+                                                        int hw, dfc* __restrict__ Gt, const dfc* __restrict__ tw_g,
+                                                        T* __restrict__ copy_out)
 {
     extern __shared__ dfc smdf[];
     const int W = 1 << logW;
@@ -61,6 +65,7 @@ __global__ void __launch_bounds__(256, 4) row_pass_kernel(const T* __restrict__ 
     const int f = blockIdx.y;
     const int y0 = blockIdx.x * kRowBlock;
     const T* fr = frames + (long long)f * fstride + (long long)y0 * W;
+    T* co = copy_out ? copy_out + (long long)f * fstride + (long long)y0 * W : nullptr;
     load_twiddles_packed(tw, tw_g, logW, kTwLog);
     auto put = [&](int idx, float2 v) {
         const int r = idx >> logW, x = idx & (W - 1);
@@ -78,13 +83,17 @@ __global__ void __launch_bounds__(256, 4) row_pass_kernel(const T* __restrict__ 
     // stores of one vector element go to 32 bit-reversed slots that the
     // padding spreads over all banks
     constexpr int PV = sizeof(T) <= 4 ? 16 / (int)sizeof(T) : 1;
-    if (PV > 1 && (reinterpret_cast<uintptr_t>(fr) & 15) == 0) {
+    if (PV > 1 && (reinterpret_cast<uintptr_t>(fr) & 15) == 0 && (reinterpret_cast<uintptr_t>(co) & 15) == 0) {
         const int vpl = W / PV; // vectors per row
         for (int i = threadIdx.x; i < (kRowBlock / 2) * vpl; i += blockDim.x) {
             const int pr = i / vpl, x0 = (i - pr * vpl) * PV;
             T p0[PV], p1[PV];
             *reinterpret_cast<uint4*>(p0) = *reinterpret_cast<const uint4*>(fr + (2 * pr) * W + x0);
             *reinterpret_cast<uint4*>(p1) = *reinterpret_cast<const uint4*>(fr + (2 * pr + 1) * W + x0);
+            if (co) {
+                *reinterpret_cast<uint4*>(co + (2 * pr) * W + x0) = *reinterpret_cast<const uint4*>(p0);
+                *reinterpret_cast<uint4*>(co + (2 * pr + 1) * W + x0) = *reinterpret_cast<const uint4*>(p1);
+            }
             dfc* L = lines + pr * LW;
 #pragma unroll
             for (int e = 0; e < PV; ++e) {
@@ -95,8 +104,11 @@ __global__ void __launch_bounds__(256, 4) row_pass_kernel(const T* __restrict__ 
             }
         }
     } else {
-        for (int idx = threadIdx.x; idx < kRowBlock * W; idx += blockDim.x)
+        for (int idx = threadIdx.x; idx < kRowBlock * W; idx += blockDim.x) {
             put(idx, pix_df(fr, idx));
+            if (co)
+                co[idx] = fr[idx];
+        }
     }
     __syncthreads();
     fft_passes(lines, logW, kRowBlock / 2, LW, tw, kTwLog, -1);
@@ -332,7 +344,7 @@ static size_t col_pass_smem(int H)
 static size_t xcorr_rows_smem(int W) { return sizeof(float2) * (W + (W / 2 + 1) * (kRowBlock + 1) + (kRowBlock / 2) * pad8(W)); }
 
 cudaError_t launch_row_pass(int dtype, const void* frames, long long fstride, int nframes, const Geometry& g, dfc* Gt,
-                            const dfc* twdf, cudaStream_t st)
+                            const dfc* twdf, cudaStream_t st, void* copy_out)
 {
     const dim3 grid(g.H / kRowBlock, nframes);
     const size_t smem = row_pass_smem(g.W), smem_max = row_pass_smem(1 << kMaxLog);
@@ -340,19 +352,23 @@ cudaError_t launch_row_pass(int dtype, const void* frames, long long fstride, in
     switch (dtype) {
     case 0:
         if ((e = allow_smem(row_pass_kernel<uint8_t>, smem_max)) != cudaSuccess) return e;
-        row_pass_kernel<uint8_t><<<grid, 256, smem, st>>>((const uint8_t*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf);
+        row_pass_kernel<uint8_t><<<grid, 256, smem, st>>>((const uint8_t*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf,
+                                                          (uint8_t*)copy_out);
         break;
     case 1:
         if ((e = allow_smem(row_pass_kernel<uint16_t>, smem_max)) != cudaSuccess) return e;
-        row_pass_kernel<uint16_t><<<grid, 256, smem, st>>>((const uint16_t*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf);
+        row_pass_kernel<uint16_t><<<grid, 256, smem, st>>>((const uint16_t*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf,
+                                                           (uint16_t*)copy_out);
         break;
     case 2:
         if ((e = allow_smem(row_pass_kernel<float>, smem_max)) != cudaSuccess) return e;
-        row_pass_kernel<float><<<grid, 256, smem, st>>>((const float*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf);
+        row_pass_kernel<float><<<grid, 256, smem, st>>>((const float*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf,
+                                                        (float*)copy_out);
         break;
     default:
         if ((e = allow_smem(row_pass_kernel<double>, smem_max)) != cudaSuccess) return e;
-        row_pass_kernel<double><<<grid, 256, smem, st>>>((const double*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf);
+        row_pass_kernel<double><<<grid, 256, smem, st>>>((const double*)frames, fstride, g.logW, g.H, g.hw, Gt, twdf,
+                                                         (double*)copy_out);
         break;
     }
     note_launches(1);

@@ -373,6 +373,13 @@ struct smip_stack {
     cudaEvent_t ev_copied[2] = { nullptr, nullptr }; // copies into stg[i] done (on cst)
     cudaEvent_t ev_free[2] = { nullptr, nullptr };   // kernels done reading stg[i] (on st)
     bool free_rec[2] = { false, false };
+    // A batch whose frames the row pass reads straight from mapped
+    // page-locked host memory (the first full batch of a push, which no
+    // earlier work could overlap with a copy); the row pass writes them into
+    // stg[cur] for the later kernels.  ev_zc: that row pass is done, so the
+    // copy stream's next transfer does not share the host link with it.
+    const void* zc_src = nullptr;
+    cudaEvent_t ev_zc = nullptr;
     double* spec_staging = nullptr; // spectra input (mode 2)
     void* ref = nullptr;          // raw frame 0
     double* ref_sq = nullptr;
@@ -419,6 +426,7 @@ struct smip_stack {
             if (ev_copied[i]) cudaEventDestroy(ev_copied[i]);
             if (ev_free[i]) cudaEventDestroy(ev_free[i]);
         }
+        if (ev_zc) cudaEventDestroy(ev_zc);
         if (cst)
             cudaStreamDestroy(cst);
         dfree(spec_staging);
@@ -540,15 +548,23 @@ struct smip_stack {
             const size_t fe = frame_elems();
             const bool first = !has_ref;
             void* staging = stg[cur];
-            if (wait_copies) {
+            const void* zc = zc_src;
+            zc_src = nullptr;
+            if (wait_copies && !zc) {
                 CUDA_TRY(cudaEventRecord(ev_copied[cur], cst));
                 CUDA_TRY(cudaStreamWaitEvent(q, ev_copied[cur], 0));
             }
             if (first) {
-                CUDA_TRY(cudaMemcpyAsync(ref, staging, dtype_size(dtype) * fe, cudaMemcpyDeviceToDevice, q));
+                CUDA_TRY(cudaMemcpyAsync(ref, zc ? zc : staging, dtype_size(dtype) * fe, cudaMemcpyDefault, q));
                 CUDA_TRY(launch_sumsq(dtype, ref, (long long)fe, ref_sq, q));
             }
-            CUDA_TRY(launch_row_pass(dtype, staging, (long long)fe, n, g, Gt, ctx->twdf, q));
+            if (zc) {
+                CUDA_TRY(launch_row_pass(dtype, zc, (long long)fe, n, g, Gt, ctx->twdf, q, staging));
+                CUDA_TRY(cudaEventRecord(ev_zc, q));
+                CUDA_TRY(cudaStreamWaitEvent(cst, ev_zc, 0));
+            } else {
+                CUDA_TRY(launch_row_pass(dtype, staging, (long long)fe, n, g, Gt, ctx->twdf, q));
+            }
             if (first)
                 CUDA_TRY(launch_col_pass(1, Gt, S, R, R, T, Ppart, 1, fpc, 0, g, ctx->twdf, ctx->tw32, q));
             CUDA_TRY(launch_col_pass(0, Gt, S, R, nullptr, T, Ppart, n, fpc, first ? 1 : 0, g, ctx->twdf, ctx->tw32,
@@ -728,7 +744,29 @@ extern "C" int smip_stack_push_frames(smip_stack_t s, const void* frames, int dt
     s->mode = 1;
     const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     const char* src = static_cast<const char*>(frames);
+    // page-locked host frames: the first full batch is read by the row pass
+    // through the mapped pointer instead of waiting for a copy
+    const char* mapped = nullptr;
+    if (!on_device && (size_t)stride_bytes == fbytes && s->pending == 0 && count >= s->Bf) {
+        cudaPointerAttributes pa {};
+        if (cudaPointerGetAttributes(&pa, frames) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+            mapped = static_cast<const char*>(pa.devicePointer);
+        else
+            cudaGetLastError(); // pageable memory: not an error
+        if (mapped && !s->ev_zc)
+            CUDA_TRY(cudaEventCreateWithFlags(&s->ev_zc, cudaEventDisableTiming));
+    }
     long done = 0;
+    if (mapped) {
+        s->zc_src = mapped;
+        s->pending = s->Bf;
+        s->nframes += s->Bf;
+        done = s->Bf;
+        if ((rc = s->run_batch())) {
+            s->zc_src = nullptr;
+            return rc;
+        }
+    }
     while (done < count) {
         const long k = std::min<long>(count - done, s->Bf - s->pending);
         if (s->pending == 0 && s->free_rec[s->cur]) // the kernels of the buffer's last batch are done with it

@@ -44,9 +44,10 @@ void set_error_message(const std::string& m);
 // All launchers are asynchronous on `st` and return cudaGetLastError().
 
 // frames (dtype) -> G'(a, y) = sum_x f(x,y) exp(+2 pi i a x / W), float-float,
-// stored [f][a][y].  dtype: 0 u8, 1 u16, 2 f32, 3 f64.
+// stored [f][a][y].  dtype: 0 u8, 1 u16, 2 f32, 3 f64.  copy_out (optional,
+// device memory): the frames as read, same stride.
 cudaError_t launch_row_pass(int dtype, const void* frames, long long frame_stride_elems, int nframes,
-                            const Geometry& g, dfc* Gt, const dfc* twdf, cudaStream_t st);
+                            const Geometry& g, dfc* Gt, const dfc* twdf, cudaStream_t st, void* copy_out = nullptr);
 
 // Column pass.  mode 1: frame 0 only -> Rout (the reference spectrum).
 // mode 0: S[f][a][c] = F(-a, c - H/2), power partials, and the FP32 inverse
