@@ -93,6 +93,17 @@ SMIP_GPU_API int smip_stack_destroy(smip_stack_t s);
 SMIP_GPU_API int smip_stack_push_frames(smip_stack_t s, const void* frames, int dtype, long count,
                                         long frame_stride_bytes, int on_device);
 
+/* Phase-recovery estimator for smip_stack_reconstruct / smip_stack_finish.
+ * SMIP_RECO_SPIRAL (default): the reference's walk (phasereco.h:33-123), each
+ * point from every pair whose phases exist when the spiral reaches it.
+ * SMIP_RECO_RINGS: not the reference's estimator -- the points of one turn of
+ * the spiral (a ring) are formed in parallel from the pairs set in earlier
+ * rings only; faster, and its phases differ from the reference's (the
+ * difference is measured, not bounded by it). */
+#define SMIP_RECO_SPIRAL 0
+#define SMIP_RECO_RINGS 1
+SMIP_GPU_API int smip_stack_set_reco_mode(smip_stack_t s, int mode);
+
 /* Replaces Bispectrum::accumulate_from_fft(const Array2<complex<double>>&)
  * (bispectrum.h:82-83, 356-409) for spectra computed elsewhere: count spectra
  * of ncols x nrows complex<double> in FFT order, host or device memory.

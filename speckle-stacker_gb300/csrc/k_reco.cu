@@ -528,6 +528,150 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
     }
 }
 
+// ------------------------------------------ ring-parallel estimator (opt-in)
+// A different estimator from the reference's spiral, offered as an option:
+// the spiral's visits are grouped by the radius r at which NextRecoIndex makes
+// them (one ring per r, each point once per ring), and every point of ring k
+// is formed in parallel from the pairs whose u and v got their phases in
+// rings before k.  The spiral also uses phases set earlier in the same ring,
+// so the two differ; the phase difference is measured, not bounded by the
+// reference.  fring[p]: the ring in which point p got its phase (seeds 0),
+// -1 while it has none; only rings < k are read while ring k is written, so
+// the result does not depend on the order in which the ring's warps run.
+__global__ void ring_seed_kernel(const RecoJob* __restrict__ jobs, int* __restrict__ fring)
+{
+    const RecoJob J = jobs[0];
+    if (threadIdx.x < 5) { // seeds (phasereco.h:42-54), as in the spiral walk
+        const int sx[5] = { 0, 1, 0, -1, 0 }, sy[5] = { 0, 0, 1, 0, -1 };
+        const int p = wrap_idx(sx[threadIdx.x], sy[threadIdx.x], J.W, J.H);
+        const float im = threadIdx.x < 3 ? 0.f : -0.f;
+        J.phf[p] = make_float2(1.f, im);
+        J.sums[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        J.cnt[p] = -1;
+        fring[p] = 0;
+    }
+}
+
+// One warp per visit of ring `ring`: rq[0..n) are the ring's visit indices.
+__global__ void __launch_bounds__(256) ring_pass_kernel(const RecoJob* __restrict__ jobs, const int* __restrict__ rq,
+                                                        int n, int ring, int* __restrict__ fring)
+{
+    const RecoJob J = jobs[0];
+    const int gw = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (gw >= n) // whole warps leave together
+        return;
+    const int W = J.W, H = J.H, De = J.De, nside = De + 1, nv = nside * nside;
+    const int q = rq[gw];
+    const int2 w = J.visits[q];
+    const int pmin0 = -(W >> 1), pmin1 = -(H >> 1);
+    const int pmax0 = -W / 2 + W - 1, pmax1 = -H / 2 + H - 1;
+    const int szW = (W / 2) * 2 + 1, szH = (H / 2) * 2 + 1;
+    const int umn0 = -(szW / 2), umx0 = szW - szW / 2 - 1, umn1 = -(szH / 2), umx1 = szH - szH / 2 - 1;
+    if (w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1)
+        return;
+    const int pw = wrap_idx(w.x, w.y, W, H);
+    if (fring[pw] >= 0 || abs(w.x) + abs(w.y) <= 1                          // phasereco.h:84
+        || w.x < umn0 || w.x > umx0 || w.y < umn1 || w.y > umx1)
+        return;
+    const float2* prow = J.plan + (long long)q * nv;
+    float sr = 0.f, si = 0.f;
+    int cnt = 0;
+    for (int t = lane; t < nv; t += 32) {
+        const float2 bh = prow[t];
+        if (bh.x == 0.f && bh.y == 0.f) // the plan's zero: never contributes
+            continue;
+        const int vx = -De / 2 + t % nside, vy = -De / 2 + t / nside;
+        const int ux = w.x - vx, uy = w.y - vy;
+        if (ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1)
+            continue;
+        const int pu = wrap_idx(ux, uy, W, H), pv = wrap_idx(vx, vy, W, H);
+        const int fu = fring[pu], fv = fring[pv];
+        if (fu < 0 || fu >= ring || fv < 0 || fv >= ring)
+            continue;
+        if (isnan(bh.x)) {
+            record_error(J.err, SMIP_DEV_ERR_OUT_OF_RANGE);
+            continue;
+        }
+        const float2 ph = cmul(cmul(J.phf[pu], J.phf[pv]), make_float2(bh.x, -bh.y));
+        const float r = rsqrtf(ph.x * ph.x + ph.y * ph.y);
+        sr += ph.x * r;
+        si += ph.y * r;
+        ++cnt;
+    }
+    float rh = sr, rl = 0.f, ih = si, il = 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
+        const float c = __shfl_xor_sync(0xffffffffu, ih, o), e = __shfl_xor_sync(0xffffffffu, il, o);
+        ff_add(rh, rl, a, b);
+        ff_add(ih, il, c, e);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    if (lane == 0 && cnt > 0) {
+        const float s2 = rh * rh + ih * ih;
+        const float lim = 2.220446049250313e-16f * (float)cnt;
+        float2 pf = make_float2(0.f, 0.f);
+        if (s2 > lim * lim) {
+            const float r = rsqrtf(s2);
+            pf = make_float2(rh * r, ih * r);
+        }
+        J.phf[pw] = pf;
+        J.sums[pw] = make_float4(rh, rl, ih, il);
+        J.cnt[pw] = cnt;
+        fring[pw] = ring;
+    }
+}
+
+// FP64 mean, consistency and phase of every point and the flag map, as the
+// spiral walk's final pass forms them.
+__global__ void ring_final_kernel(const RecoJob* __restrict__ jobs, const int* __restrict__ fring)
+{
+    const RecoJob J = jobs[0];
+    const int np = J.W * J.H;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+        const unsigned char f = fring[p] >= 0 ? 1 : 0;
+        J.flags[p] = f;
+        if (!f)
+            continue;
+        const int n = J.cnt[p];
+        if (n < 0) {
+            J.phases[p] = make_double2(1.0, J.phf[p].y);
+            J.cons[p] = 1.0;
+            continue;
+        }
+        const float4 s = J.sums[p];
+        const double mr = ((double)s.x + (double)s.y) / (double)n;
+        const double mi = ((double)s.z + (double)s.w) / (double)n;
+        const double ab = sqrt(mr * mr + mi * mi);
+        J.cons[p] = ab;
+        J.phases[p] = ab > 2.220446049250313080847263336181640625e-16 ? make_double2(mr / ab, mi / ab)
+                                                                      : make_double2(0.0, 0.0);
+    }
+}
+
+cudaError_t launch_ring_reco(const RecoJob* job_dev, int* fring, const int* rq, const std::vector<int>& roff, int W,
+                             int H, cudaStream_t st)
+{
+    reco_plan_kernel<<<dim3(1024, 1), 256, 0, st>>>(job_dev);
+    note_launches(1);
+    cudaError_t e = cudaMemsetAsync(fring, 0xff, sizeof(int) * (size_t)W * H, st); // -1: no phase yet
+    if (e != cudaSuccess)
+        return e;
+    ring_seed_kernel<<<1, 32, 0, st>>>(job_dev, fring);
+    note_launches(1);
+    for (size_t k = 1; k + 1 < roff.size(); ++k) {
+        const int n = roff[k + 1] - roff[k];
+        if (n <= 0)
+            continue;
+        ring_pass_kernel<<<(n * 32 + 255) / 256, 256, 0, st>>>(job_dev, rq + roff[k], n, (int)k, fring);
+        note_launches(1);
+    }
+    const int np = W * H;
+    ring_final_kernel<<<(np + 255) / 256 < 2048 ? (np + 255) / 256 : 2048, 256, 0, st>>>(job_dev, fring);
+    note_launches(1);
+    return cudaGetLastError();
+}
+
 // Runs the device get_element index replica on a list of 4-index tuples.
 __global__ void bispec_offset_probe_kernel(BispecDims d, const int4* __restrict__ idx, long long n,
                                            long long* __restrict__ off, int* __restrict__ conj)

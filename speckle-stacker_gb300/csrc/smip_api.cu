@@ -183,8 +183,9 @@ void next_reco_index(double& r, double& phi, int& i, int& j)
     j = jj;
 }
 
-// phasereco.h:56-68
-std::vector<int2> reco_visits(double R)
+// phasereco.h:56-68.  ring (optional): per visit the radius r at which
+// NextRecoIndex made it (r grows by 1 per turn of the spiral).
+std::vector<int2> reco_visits(double R, std::vector<int>* ring = nullptr)
 {
     std::vector<int2> v;
     double r = 0.0, phi = 0.0;
@@ -192,6 +193,8 @@ std::vector<int2> reco_visits(double R)
     while (r <= R) {
         next_reco_index(r, phi, i, j);
         v.push_back(make_int2(i, j));
+        if (ring)
+            ring->push_back((int)r);
     }
     return v;
 }
@@ -208,6 +211,10 @@ struct Reco {
     Geometry g {};
     double R = -1.0;
     int2* visits = nullptr;
+    int mode = 0;                 // 0: the reference's spiral walk; 1: ring-parallel estimator
+    int* fring = nullptr;         // ring mode: per point the ring that set its phase (-1: none)
+    int* rq = nullptr;            // ring mode: visit indices grouped by ring
+    std::vector<int> roff;        // ring k: rq[roff[k] .. roff[k+1])
     int4* pvis = nullptr;         // per point: first three visit indices, visit count
     unsigned* rbits = nullptr;    // per visit: recent pair slots (bitmask)
     int* rcount = nullptr;
@@ -224,6 +231,8 @@ struct Reco {
     ~Reco()
     {
         dfree(visits);
+        dfree(fring);
+        dfree(rq);
         dfree(pvis);
         dfree(rbits);
         dfree(rcount);
@@ -250,8 +259,37 @@ struct Reco {
             CUDA_TRY(cudaMalloc(&job, sizeof(RecoJob)));
         }
         if (radius != R) {
-            std::vector<int2> v = reco_visits(radius);
+            std::vector<int> vring;
+            std::vector<int2> v = reco_visits(radius, &vring);
             CUDA_TRY(cudaStreamSynchronize(st));
+            dfree(rq);
+            {   // ring lists: each point once per ring, in visit order
+                const int nr = vring.empty() ? 1 : vring.back() + 1;
+                std::vector<std::vector<int>> per(nr + 1);
+                std::vector<int> seen(np, -1);
+                const int qmin0 = -(g.W >> 1), qmin1 = -(g.H >> 1), qmax0 = g.W - 1 + qmin0, qmax1 = g.H - 1 + qmin1;
+                for (size_t q = 0; q < v.size(); ++q) {
+                    const int2 w = v[q];
+                    if (w.x < qmin0 || w.x > qmax0 || w.y < qmin1 || w.y > qmax1)
+                        continue;
+                    const size_t p = (size_t)(w.x < 0 ? w.x + g.W : w.x) + (size_t)(w.y < 0 ? w.y + g.H : w.y) * g.W;
+                    const int k = std::max(1, vring[q]);
+                    if (seen[p] == k)
+                        continue;
+                    seen[p] = k;
+                    per[k].push_back((int)q);
+                }
+                std::vector<int> flat;
+                roff.assign(per.size() + 1, 0);
+                for (size_t k = 0; k < per.size(); ++k) {
+                    roff[k] = (int)flat.size();
+                    flat.insert(flat.end(), per[k].begin(), per[k].end());
+                }
+                roff[per.size()] = (int)flat.size();
+                CUDA_TRY(cudaMalloc(&rq, sizeof(int) * std::max<size_t>(1, flat.size())));
+                if (!flat.empty())
+                    CUDA_TRY(cudaMemcpy(rq, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice));
+            }
             dfree(visits);
             dfree(plan);
             dfree(pvis);
@@ -307,7 +345,13 @@ struct Reco {
         j.rcount = rcount;
         j.rlist = rlist;
         CUDA_TRY(cudaMemcpyAsync(job, &j, sizeof(RecoJob), cudaMemcpyHostToDevice, st));
-        CUDA_TRY(launch_phase_reco(job, 1, g.W, g.H, g.De, st));
+        if (mode == 1) {
+            if (!fring)
+                CUDA_TRY(cudaMalloc(&fring, sizeof(int) * np));
+            CUDA_TRY(launch_ring_reco(job, fring, rq, roff, g.W, g.H, st));
+        } else {
+            CUDA_TRY(launch_phase_reco(job, 1, g.W, g.H, g.De, st));
+        }
         return SMIP_OK;
     }
     int download(double* ph, unsigned char* fl, double* cs, cudaStream_t st)
@@ -785,6 +829,18 @@ extern "C" int smip_stack_push_frames(smip_stack_t s, const void* frames, int dt
                 return rc;
         }
     }
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_set_reco_mode(smip_stack_t s, int mode)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    if (mode != SMIP_RECO_SPIRAL && mode != SMIP_RECO_RINGS)
+        return fail(SMIP_E_INVALID_ARGUMENT, "unknown phase-recovery mode");
+    CUDA_TRY(cudaStreamSynchronize(s->rst ? s->rst : s->st));
+    s->reco.mode = mode;
     return SMIP_OK;
 }
 

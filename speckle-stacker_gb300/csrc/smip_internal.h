@@ -1,6 +1,8 @@
 // smip_internal.h -- declarations shared by the SMIP host runtime and kernels.
 #pragma once
 
+#include <vector>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 #include <string>
@@ -126,6 +128,10 @@ struct RecoJob {
 constexpr int kRecoLag = 32;     // visits between a point's phase and the parallel stage's use of it
 constexpr int kRecentMax = 64;   // recent pairs per visit the serial warp takes from a list
 cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int max_H, int max_De, cudaStream_t st);
+// Ring-parallel estimator (opt-in, not the reference's): rq holds the spiral's
+// visit indices grouped by ring, ring k at [roff[k], roff[k+1]); fring: W*H ints.
+cudaError_t launch_ring_reco(const RecoJob* job_dev, int* fring, const int* rq, const std::vector<int>& roff, int W,
+                             int H, cudaStream_t st);
 // get_element index replica over a list of (ux, uy, vx, vy) tuples
 cudaError_t launch_offset_probe(const Geometry& g, const int* idx, long long n, long long* off, int* conj,
                                 cudaStream_t st);

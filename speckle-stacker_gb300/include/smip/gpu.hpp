@@ -165,6 +165,8 @@ public:
     void flush() { check(smip_stack_flush(handle())); }
     void sync() { check(smip_stack_sync(handle())); }
     void reset() { check(smip_stack_reset(handle())); }
+    // SMIP_RECO_SPIRAL (the reference's walk, default) or SMIP_RECO_RINGS (ring-parallel, not the reference's)
+    void set_reco_mode(int mode) { check(smip_stack_set_reco_mode(handle(), mode)); }
     long nframes() const
     {
         long n = 0;

@@ -121,6 +121,7 @@ def _load():
                                  C.POINTER(C.c_longlong), ip], C.c_int),
         "smip_xcorr_displacement_noalloc": ([vp, vp, C.c_long, C.c_long, vp, vp], C.c_int),
         "smip_stack_reset": ([vp], C.c_int),
+        "smip_stack_set_reco_mode": ([vp, C.c_int], C.c_int),
         "smip_stack_set_timing": ([vp, C.c_int], C.c_int),
         "smip_stack_kernel_time": ([vp, dp, lp, dp], C.c_int),
         "smip_kernel_launches": ([], C.c_longlong),
@@ -252,6 +253,13 @@ class Stack:
         if a.ndim == 2:
             a = a[None]
         _check(_L().smip_stack_accumulate_fft(self._h, a.ctypes.data, a.shape[0], 0))
+
+    def set_reco_mode(self, mode="spiral"):
+        """Phase-recovery estimator: "spiral" (default, the reference's walk)
+        or "rings" (each turn of the spiral in parallel from earlier turns
+        only: faster, not the reference's estimator)."""
+        m = {"spiral": 0, "rings": 1}.get(mode, mode)
+        _check(_L().smip_stack_set_reco_mode(self._h, int(m)))
 
     def reset(self):
         """Zero the accumulators for a new job (device buffers are kept)."""

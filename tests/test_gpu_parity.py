@@ -276,6 +276,38 @@ def test_host_device_and_page_locked_sources_agree(smip, dtype):
             assert np.array_equal(o[k], outs[0][k]), k
 
 
+@pytest.mark.parametrize("name,nframes", [("binary128", 40), ("extended256", 16)])
+def test_ring_mode_estimator(smip, oracle, name, nframes):
+    """The opt-in ring-parallel estimator on the same stack as the spiral
+    walk: the same points get phases, the reconstructed image's magnitude
+    stays within 1 % (rel-L2) of the FP64 oracle's (measured: 0.5 % at 128²,
+    0.2 % at 256²), repeat runs are bit-identical, and switching back gives
+    the spiral's results exactly."""
+    from smip_gb300 import synthetic as S
+
+    spec = S.config_spec(name, nframes=nframes)
+    frames = S.make_stack(spec)
+    n, R = frames.shape[1], float(spec.reco_radius)
+    exp = oracle.run_stack(frames, spec.bdepth, R, fp64=True, nthreads=16)
+    with smip.Stack(n, n, spec.bdepth) as st:
+        st.push_frames(frames)
+        sp = st.finish(R)
+        st.set_reco_mode("rings")
+        r1 = st.finish(R)
+        r2 = st.finish(R)
+        st.set_reco_mode("spiral")
+        sp2 = st.finish(R)
+    for a, b in zip(r1, r2):
+        assert np.array_equal(a, b)
+    for a, b in zip(sp, sp2):
+        assert np.array_equal(a, b)
+    assert np.array_equal(r1[2], exp["flags"])
+    assert rel_l2(np.abs(r1[0]), np.abs(exp["image"])) <= 1e-2
+    with pytest.raises(smip.InvalidArgument):
+        with smip.Stack(n, n, spec.bdepth) as st:
+            st.set_reco_mode(7)
+
+
 def test_single_frame_and_errors(smip, oracle):
     from smip_gb300 import synthetic as S
 
