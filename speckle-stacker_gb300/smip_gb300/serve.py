@@ -140,11 +140,14 @@ class Engine:
         reconstructions start, instead of one flush per job.
     stall_timeout: seconds a streaming job may go without new frames from its
         producer before it fails (None: wait for ever).
+    reco_mode: "spiral" (the reference's phase recovery, default) or "rings"
+        (the opt-in ring-parallel estimator, Stack.set_reco_mode).
     """
 
     def __init__(self, device: int = 0, budget_bytes: float = 120e9, max_active: int = 64, workers: int = 32,
                  stack_factory: Optional[Callable] = None, graph: bool = False,
-                 batch_launch: Optional[Callable] = None, stall_timeout: Optional[float] = None):
+                 batch_launch: Optional[Callable] = None, stall_timeout: Optional[float] = None,
+                 reco_mode: str = "spiral"):
         if stack_factory is None:
             from smip_gb300 import Stack
 
@@ -159,6 +162,7 @@ class Engine:
         self.max_active = int(max_active)
         self.workers = int(workers)
         self.stall_timeout = stall_timeout
+        self.reco_mode = reco_mode
         self.pool: Dict[Tuple[int, int, int], list] = {}
         self.peak_bytes = 0.0
         self.peak_active = 0
@@ -187,7 +191,10 @@ class Engine:
 
     def _acquire(self, shape):
         lst = self.pool.setdefault(shape, [])
-        return lst.pop() if lst else self.factory(*shape)
+        st = lst.pop() if lst else self.factory(*shape)
+        if self.reco_mode != "spiral":
+            st.set_reco_mode(self.reco_mode)
+        return st
 
     def _release(self, shape, st):
         try:

@@ -32,6 +32,9 @@ class FakeStack:
     def reset(self):
         self.frames = []
 
+    def set_reco_mode(self, mode):
+        self.mode = mode
+
 
 def _jobs(n, rate=None, seed=1):
     rng = np.random.default_rng(seed)
@@ -292,3 +295,16 @@ def test_engine_cancel_while_streaming_and_waiting():
     assert by_id[50].error == "cancelled" and by_id[50].nframes == 8
     assert by_id[51].error == "cancelled" and by_id[51].nframes == 0
     assert all(by_id[j.id].error is None for j in jobs[:4])
+
+
+def test_engine_reco_mode_reaches_every_stack():
+    made = []
+
+    def factory(nc, nr, d):
+        st = FakeStack(nc, nr, d)
+        made.append(st)
+        return st
+
+    eng = serve.Engine(max_active=3, workers=2, stack_factory=factory, reco_mode="rings")
+    res, _ = eng.run(_jobs(8), realtime=False)
+    assert len(res) == 8 and made and all(getattr(st, "mode", None) == "rings" for st in made)
