@@ -12,8 +12,10 @@
 // reference, -r, -k, -s, --no-calcsum and --no-specklemasking are parsed and
 // have no effect (main.cpp:84-90, 136-167 never use them).
 //
-// --apply-ignored (not a reference flag) makes them take effect as their help
-// text describes: -r idx makes frame idx the cross-correlation reference (it
+// --rings (not a reference flag) selects the ring-parallel phase recovery.
+//
+// --apply-ignored (not a reference flag) makes those five take effect as their
+// help text describes: -r idx makes frame idx the cross-correlation reference (it
 // is accumulated first, then the others in order); -k l:t and -s w:h crop
 // every frame to that box before ingest (the box must lie inside the frame;
 // its size follows the stack's power-of-two rule); --no-calcsum leaves out the
@@ -77,6 +79,8 @@ void usage(const char* progname)
               << "     -k   --croppos <l:t>         :   fixed crop box position (default: 0:0)\n"
               << "     -s   --cropsize <w:h>        :   crop box size (default: total image)\n"
               << "     -v   --verbose               :   increase verbosity level\n"
+              << "          --rings                 :   ring-parallel phase recovery (faster; not the reference's\n"
+              << "                                      estimator: each spiral turn from earlier turns only)\n"
               << "          --apply-ignored         :   make -r, -k, -s, --no-calcsum and --no-specklemasking\n"
               << "                                      take effect (the reference parses and ignores them)\n"
               << "          --version               :   display version and exit\n"
@@ -323,6 +327,7 @@ int main(int argc, char* argv[])
     int swCalcSum { 1 };
     int swShowVersion { 0 };
     int swApplyIgnored { 0 };
+    int swRings { 0 };
     std::size_t ref_frame { 0 };
     long crop_l = -1, crop_t = -1, crop_w = -1, crop_h = -1;
     std::size_t verbose { 0 };
@@ -344,6 +349,7 @@ int main(int argc, char* argv[])
                 { "no-specklemasking", no_argument, &swSpeckleMasking, 0 },
                 { "specklemasking", no_argument, &swSpeckleMasking, 1 },
                 { "apply-ignored", no_argument, &swApplyIgnored, 1 },
+                { "rings", no_argument, &swRings, 1 },
                 { 0, 0, 0, 0 }
             };
             int option_index { 0 };
@@ -495,6 +501,8 @@ int main(int argc, char* argv[])
             st.write_to_file("bispectrum.dat");
 
             info() << "reconstructing fourier phases from bispectrum\n";
+            if (swRings)
+                st.set_reco_mode(SMIP_RECO_RINGS);
             const auto res = st.finish((double)reco_radius);
             // main.cpp:329-331: phases windowed by Hann of aperture 2R for the outputs
             const auto win = smip::gpu::Hann<double>(cols, rows, (double)reco_radius * 2);

@@ -77,7 +77,7 @@ def test_cli_apply_ignored_checks_arguments(tmp_path):
     work (without the switch both are ignored, as in the reference)."""
     _need_cli()
     out = subprocess.run([CLI, "-h"], capture_output=True, text=True, check=True)
-    assert "--apply-ignored" in out.stdout
+    assert "--apply-ignored" in out.stdout and "--rings" in out.stdout
     src = tmp_path / "s.npy"
     np.save(src, np.zeros((2, 32, 32), np.uint8))
     r = subprocess.run([CLI, "--apply-ignored", "-k", "20:0", "-s", "16:16", str(src)], capture_output=True,
