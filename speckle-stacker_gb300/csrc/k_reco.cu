@@ -576,27 +576,44 @@ __global__ void __launch_bounds__(256) ring_pass_kernel(const RecoJob* __restric
     const float2* prow = J.plan + (long long)q * nv;
     float sr = 0.f, si = 0.f;
     int cnt = 0;
-    for (int t = lane; t < nv; t += 32) {
-        const float2 bh = prow[t];
-        if (bh.x == 0.f && bh.y == 0.f) // the plan's zero: never contributes
-            continue;
-        const int vx = -De / 2 + t % nside, vy = -De / 2 + t / nside;
-        const int ux = w.x - vx, uy = w.y - vy;
-        if (ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1)
-            continue;
-        const int pu = wrap_idx(ux, uy, W, H), pv = wrap_idx(vx, vy, W, H);
-        const int fu = fring[pu], fv = fring[pv];
-        if (fu < 0 || fu >= ring || fv < 0 || fv >= ring)
-            continue;
-        if (isnan(bh.x)) {
-            record_error(J.err, SMIP_DEV_ERR_OUT_OF_RANGE);
-            continue;
+    // kB slots per lane at a time: every gather of the group is issued before
+    // any is used, so their latencies overlap; the sums take the slots in
+    // increasing order as a one-slot loop would
+    constexpr int kB = 8;
+    for (int t0 = lane; t0 < nv; t0 += 32 * kB) {
+        float2 bh[kB], pa[kB], pb[kB];
+        int fu[kB], fv[kB];
+        bool use[kB];
+#pragma unroll
+        for (int k = 0; k < kB; ++k) {
+            const int t = t0 + 32 * k;
+            use[k] = t < nv;
+            bh[k] = use[k] ? prow[t] : make_float2(0.f, 0.f);
+            const int vx = -De / 2 + t % nside, vy = -De / 2 + t / nside;
+            const int ux = w.x - vx, uy = w.y - vy;
+            use[k] = use[k] && !(ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1);
+            const int pu = use[k] ? wrap_idx(ux, uy, W, H) : 0, pv = use[k] ? wrap_idx(vx, vy, W, H) : 0;
+            fu[k] = use[k] ? fring[pu] : -1;
+            fv[k] = use[k] ? fring[pv] : -1;
+            pa[k] = use[k] ? J.phf[pu] : make_float2(0.f, 0.f);
+            pb[k] = use[k] ? J.phf[pv] : make_float2(0.f, 0.f);
         }
-        const float2 ph = cmul(cmul(J.phf[pu], J.phf[pv]), make_float2(bh.x, -bh.y));
-        const float r = rsqrtf(ph.x * ph.x + ph.y * ph.y);
-        sr += ph.x * r;
-        si += ph.y * r;
-        ++cnt;
+#pragma unroll
+        for (int k = 0; k < kB; ++k) {
+            if (!use[k] || (bh[k].x == 0.f && bh[k].y == 0.f)) // the plan's zero: never contributes
+                continue;
+            if (fu[k] < 0 || fu[k] >= ring || fv[k] < 0 || fv[k] >= ring)
+                continue;
+            if (isnan(bh[k].x)) {
+                record_error(J.err, SMIP_DEV_ERR_OUT_OF_RANGE);
+                continue;
+            }
+            const float2 ph = cmul(cmul(pa[k], pb[k]), make_float2(bh[k].x, -bh[k].y));
+            const float r = rsqrtf(ph.x * ph.x + ph.y * ph.y);
+            sr += ph.x * r;
+            si += ph.y * r;
+            ++cnt;
+        }
     }
     float rh = sr, rl = 0.f, ih = si, il = 0.f;
 #pragma unroll
