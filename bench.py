@@ -301,6 +301,9 @@ def serving_metrics(jobs):
         runs_s = [eng.run(jl, realtime=realtime) for _ in range(2)]
         runs_g = [eng_g.run(jl, realtime=realtime) for _ in range(2)]
         runs_p = [serve.run_plain(jl, realtime=realtime) for _ in range(2)]
+        eng.reco_mode = "rings"  # the opt-in ring-parallel phase recovery, same engine
+        runs_r = [eng.run(jl, realtime=realtime) for _ in range(2)]
+        eng.reco_mode = "spiral"
         res_s, span_s = min(runs_s, key=lambda x: x[1])
         res_g, span_g = min(runs_g, key=lambda x: x[1])
         res_p, span_p = min(runs_p, key=lambda x: x[1])
@@ -311,7 +314,8 @@ def serving_metrics(jobs):
                     "results_identical": serve.compare_results(res_s, res_p),
                     "peak_jobs_in_flight": eng.peak_active,
                     "served_graph": sg, "frames_per_s_ratio_graph": sg["frames_per_s"] / p["frames_per_s"],
-                    "results_identical_graph": serve.compare_results(res_g, res_p)}
+                    "results_identical_graph": serve.compare_results(res_g, res_p),
+                    "served_rings": serve.summarize(*min(runs_r, key=lambda x: x[1]))}
         del eng, eng_g
     del keep
     return out

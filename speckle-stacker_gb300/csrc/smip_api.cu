@@ -839,8 +839,7 @@ extern "C" int smip_stack_set_reco_mode(smip_stack_t s, int mode)
         return rc;
     if (mode != SMIP_RECO_SPIRAL && mode != SMIP_RECO_RINGS)
         return fail(SMIP_E_INVALID_ARGUMENT, "unknown phase-recovery mode");
-    CUDA_TRY(cudaStreamSynchronize(s->rst ? s->rst : s->st));
-    s->reco.mode = mode;
+    s->reco.mode = mode; // read on the host when the next reconstruction is issued
     return SMIP_OK;
 }
 

@@ -192,8 +192,9 @@ class Engine:
     def _acquire(self, shape):
         lst = self.pool.setdefault(shape, [])
         st = lst.pop() if lst else self.factory(*shape)
-        if self.reco_mode != "spiral":
-            st.set_reco_mode(self.reco_mode)
+        setter = getattr(st, "set_reco_mode", None)
+        if callable(setter):  # pooled stacks may come from a run in the other mode
+            setter(self.reco_mode)
         return st
 
     def _release(self, shape, st):
