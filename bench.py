@@ -187,20 +187,21 @@ def cpu_baseline(frames, depth, budget_s=12.0, threads=None):
                       f"bispectrum d={depth}), {el:.1f} s"}
 
 
-def accuracy_check(G, spec, device, nframes=16, threads=None):
-    """The oracle as the checker: the first ``nframes`` frames of the workload
-    through the GPU stack and through the FP64 oracle (same seeded frames,
-    the workload's depth and reco radius); the errors the parity tests bound."""
+def accuracy_check(G, spec, frames, device, threads=None):
+    """The oracle as the checker: the given first frames of the workload (one
+    whole batch of the library's default size, so that the in-register batch
+    sum is as long as in the timed run) through the GPU stack and through the
+    FP64 oracle, with the workload's depth and reco radius; the errors the
+    parity tests bound."""
     from oracle import Oracle
 
-    from smip_gb300 import synthetic as S
-
     threads = threads or os.cpu_count() or 1
-    sample = S.make_stack(spec, 0, nframes)
+    sample = np.ascontiguousarray(frames)
+    nframes = len(sample)
     R = float(spec.reco_radius)
     exp = Oracle().run_stack(sample, spec.bdepth, R, fp64=True, nthreads=threads)
     n = sample.shape[1]
-    with G.Stack(n, n, spec.bdepth, device=device, batch_frames=8) as st:
+    with G.Stack(n, n, spec.bdepth, device=device) as st:
         st.push_frames(sample)
         sh, sm, pw, bs = st.shifts(), st.sum(), st.power(), st.bispectrum()
         img, ph, fl, _ = st.finish(R)
@@ -489,7 +490,8 @@ def run_ours(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(frames, D)
-        cpu["check"] = accuracy_check(G, spec, local, nframes=16 if n <= 256 else 4)
+        # one whole default batch: 1024 frames at 256x256, 288 at 512x512
+        cpu["check"] = accuracy_check(G, spec, frames[:1024 if n <= 256 else 288], local)
     serving = serving_metrics(serve_jobs) if serve_jobs else None
     line = {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
@@ -507,6 +509,13 @@ def run_ours(args):
         "frame_generation_s": t_gen,
     }
     if serving:
+        for k in ("batched", "served"):
+            if k in serving and "served_rings" in serving[k]:
+                serving[k]["served_rings"].update({
+                    "estimator": "opt-in ring-parallel phase recovery, not the reference's",
+                    "phase_rms_rad_vs_spiral": recon["rings"]["phase_rms_rad_vs_spiral"],
+                    "meets_1e-3_rad_target": recon["rings"]["phase_rms_rad_vs_spiral"] <= 1e-3,
+                    "note": "reported for information only; no requirement figure uses it"})
         line.update(serving)
     st.close()
     if rank == 0:

@@ -22,6 +22,9 @@ import subprocess
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+# The reference source tree (read only by the build recipe and by tests that
+# use its sample data); the SMIP_REFERENCE environment variable overrides it.
+REFERENCE = os.environ.get("SMIP_REFERENCE", "/root/reference")
 BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 
@@ -37,7 +40,7 @@ _ubp = C.POINTER(C.c_ubyte)
 def build(reference: str | None = None) -> None:
     """Compile the oracle (and the reference build when its sources exist)."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    ref = reference or "/root/reference"
+    ref = reference or REFERENCE
     if os.path.isdir(os.path.join(ref, "include")):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE={ref}"], check=True)
 
@@ -159,6 +162,8 @@ class Oracle(_Common):
         L.orc_shifted.argtypes = [_dp, _dp, C.c_long, C.c_long, C.c_int, C.c_int]
         L.orc_general_hamming.argtypes = [_dp, C.c_long, C.c_long, C.c_double, C.c_double]
         L.orc_fft_2d.argtypes = [_dp, C.c_long, C.c_long, C.c_int]
+        L.orc_map_to_color_u16.argtypes = [_dp, C.c_long, C.POINTER(C.c_uint16)]
+        L.orc_array2mat_order.argtypes = [_dp, _dp, C.c_long, C.c_long, C.c_int]
         L.orc_fft_r2c_2d.argtypes = [_dp, _dp, C.c_long, C.c_long]
         L.orc_fft_c2r_2d.argtypes = [_dp, _dp, C.c_long, C.c_long]
         L.orc_run_stack.argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_long, C.c_long, C.c_long, C.c_double,
@@ -213,6 +218,20 @@ class Oracle(_Common):
     def hann(self, xsize, ysize, aperture, alpha=0.5):
         out = np.zeros((ysize, xsize), np.float64)
         self.lib.orc_general_hamming(_ptr(out, _dp), xsize, ysize, float(aperture), float(alpha))
+        return out
+
+    def map_to_color(self, v):
+        """mapToColor<uint16_t> (videoio.h:178-206) of every value: (..., 3) r, g, b."""
+        v = np.ascontiguousarray(v, np.float64)
+        out = np.zeros(v.shape + (3,), np.uint16)
+        self.lib.orc_map_to_color_u16(_ptr(v, _dp), v.size, out.ctypes.data_as(C.POINTER(C.c_uint16)))
+        return out
+
+    def array2mat_order(self, a, signed_symmetry):
+        """Array2Mat's pixel order (videoio.h:137-146) of a real (nrows, ncols) array."""
+        a = np.ascontiguousarray(a, np.float64)
+        out = np.zeros_like(a)
+        self.lib.orc_array2mat_order(_ptr(a, _dp), _ptr(out, _dp), a.shape[1], a.shape[0], int(signed_symmetry))
         return out
 
     def fft2(self, a, sign=-1):

@@ -666,6 +666,48 @@ void orc_general_hamming(double* out, long xsize, long ysize, double aperture, d
 }
 
 /* ------------------------------------------------------------------------ */
+/* output mapping: include/videoio.h:100-156, 178-206                        */
+/* ------------------------------------------------------------------------ */
+void orc_map_to_color_u16(const double* v, long n, uint16_t* rgb)
+{
+    const double M = 65535.0; /* std::numeric_limits<uint16_t>::max() */
+    for (long q = 0; q < n; ++q) {
+        double x = v[q];
+        x = isnan(x) ? 0.0 : (x < 0.0 ? 0.0 : (x > 1.0 ? 1.0 : x)); /* std::clamp(value, 0., 1.) */
+        double r, g, b;
+        if (x < 0.25) { /* blue rises */
+            r = 0.0; g = 0.0; b = M * (4.0 * x);
+        } else if (x < 0.5) { /* green rises, blue falls */
+            r = 0.0; g = M * (4.0 * x - 1.0); b = M * (2.0 - 4.0 * x);
+        } else if (x < 0.75) { /* red rises, green falls */
+            r = M * (4.0 * x - 2.0); g = M * (3.0 - 4.0 * x); b = 0.0;
+        } else { /* red full, blue rises again */
+            r = M; g = 0.0; b = M * (4.0 * x - 3.0);
+        }
+        /* static_cast<uint16_t>: truncation toward zero */
+        rgb[3 * q] = (uint16_t)r;
+        rgb[3 * q + 1] = (uint16_t)g;
+        rgb[3 * q + 2] = (uint16_t)b;
+    }
+}
+
+void orc_array2mat_order(const double* in, double* out, long ncols, long nrows, int signed_symmetry)
+{
+    const long minx = -(ncols / 2), miny = -(nrows / 2); /* Array2::min_sindices */
+    for (long i = 0; i < nrows; ++i)
+        for (long j = 0; j < ncols; ++j) {
+            long sx = j, sy = i;
+            if (signed_symmetry) { /* arr.at({jj, ii}), negative indices wrapped by +size */
+                sx = j + minx;
+                sy = i + miny;
+                sx = sx < 0 ? sx + ncols : sx;
+                sy = sy < 0 ? sy + nrows : sy;
+            }
+            out[i * ncols + j] = in[sy * ncols + sx];
+        }
+}
+
+/* ------------------------------------------------------------------------ */
 /* pipeline: smip-cli/main.cpp:246-378                                       */
 /* ------------------------------------------------------------------------ */
 static double pixel(const void* frames, int dtype, long n)

@@ -90,6 +90,16 @@ void orc_shifted(const double* in, double* out, long ncols, long nrows, int dx, 
 /* ---- GeneralHamming / Hann: include/window_function.h:70-85 ---- */
 void orc_general_hamming(double* out, long xsize, long ysize, double aperture, double alpha);
 
+/* ---- output mapping: Array2Mat (include/videoio.h:100-156) ----
+ * mapToColor<uint16_t> (include/videoio.h:178-206): n values, clamped to
+ * [0, 1], to 16-bit (r, g, b) triples, 3*n values written as r, g, b (the
+ * PNG order of the reference's BGR cv::Mat).  A NaN value maps as 0. */
+void orc_map_to_color_u16(const double* v, long n, uint16_t* rgb);
+/* Array2Mat's pixel order (videoio.h:137-146): pixel (x, y) of the output
+ * shows element (x + min_x, y + min_y) of the signed index range when
+ * signed_symmetry is set (an fftshift), element (x, y) otherwise. */
+void orc_array2mat_order(const double* in, double* out, long ncols, long nrows, int signed_symmetry);
+
 /* ---- whole pipeline: smip-cli/main.cpp:246-378 (without OpenCV) ----
  * frames: nframes frames, ncols x nrows, dtype 0=u8 1=u16 2=f32 3=f64,
  *         frame stride = ncols*nrows elements.

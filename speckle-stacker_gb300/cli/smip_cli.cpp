@@ -25,14 +25,17 @@
 //
 // Input: the reference decodes video/GIF with OpenCV (videoio.h:38-98); here
 // <source> is an animated GIF (decoded by gif_decode.hpp into BGR frames, the
-// order OpenCV delivers) or a NumPy .npy frame stack, uint8/uint16/float32/
-// float64, shape [frames][rows][cols] or [frames][rows][cols][channels].  For a
+// order OpenCV delivers), a SER or uncompressed AVI recording (video_decode.hpp:
+// 8 or 16-bit mono, or colour in BGR order), or a NumPy .npy frame stack,
+// uint8/uint16/float32/float64, shape [frames][rows][cols] or
+// [frames][rows][cols][channels].  For a
 // multi-channel stack -c picks channel clamp(round(log2(c)), 0, channels-1)
 // with r=1, g=2, b=4, i=7 (videoio.h:78-79), as Mat2Array does (so on BGR
 // frames "r" reads the first channel, as the reference's does).
 #include <getopt.h>
 
 #include "gif_decode.hpp"
+#include "video_decode.hpp"
 
 #include <algorithm>
 #include <array>
@@ -44,6 +47,7 @@
 #include <cstring>
 #include <iostream>
 #include <limits>
+#include <memory>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -97,6 +101,7 @@ struct Npy {
     std::vector<std::size_t> shape;
     long data_off = 0;
     std::vector<std::uint8_t> mem; // decoded frames (a GIF), used instead of the file when set
+    std::shared_ptr<smipcli::VideoSource> video; // SER / AVI frames, read one at a time when set
     ~Npy()
     {
         if (f)
@@ -299,7 +304,9 @@ void push_chunk(smip::gpu::Stack& st, Npy& n, const std::vector<std::size_t>& or
     std::vector<T> out(cr.w * cr.h * count);
     for (std::size_t k = 0; k < count; ++k) {
         const std::size_t idx = order[first + k];
-        if (!n.mem.empty()) {
+        if (n.video) {
+            n.video->read_frame(idx, in.data());
+        } else if (!n.mem.empty()) {
             std::memcpy(in.data(), n.mem.data() + idx * fe * sizeof(T), fe * sizeof(T));
         } else {
             std::fseek(n.f, n.data_off + (long)(idx * fe * sizeof(T)), SEEK_SET);
@@ -426,6 +433,17 @@ int main(int argc, char* argv[])
             npy.esize = 1;
             npy.shape = { gf.count, gf.height, gf.width, 3 };
             npy.mem = std::move(gf.bgr);
+        } else if (smipcli::VideoSource::is_ser(filename) || smipcli::VideoSource::is_avi(filename)) {
+            // SER / uncompressed AVI: one channel, or three in B, G, R order; 8 or 16-bit samples
+            auto v = std::make_shared<smipcli::VideoSource>(smipcli::VideoSource::is_ser(filename)
+                                                                ? smipcli::VideoSource::open_ser(filename)
+                                                                : smipcli::VideoSource::open_avi(filename));
+            npy.kind = 'u';
+            npy.esize = v->esize;
+            npy.shape = { v->count, v->height, v->width };
+            if (v->channels > 1)
+                npy.shape.push_back(v->channels);
+            npy.video = v;
         } else {
             open_npy(npy, filename);
         }

@@ -10,15 +10,23 @@
 // output, and every intermediate buffer lives in the fixed array below.
 //
 // The array is a file-scope __device__ object of kScratchBytes (about 3 MB,
-// enough for frames up to 256 x 256).  Every GPU that loads this library holds
-// it until the process exits.  Host code may not use its name as an address,
-// so the first call on each device looks the address up with
-// cudaGetSymbolAddress (with that device current) and copies the FFT twiddle
-// tables into it; that first call should therefore come before any stream
-// capture.  All calls on a device share the array: two calls whose work
-// overlaps on the GPU race with each other and must be ordered by the caller
-// (one stream, or events).  Each call writes every scratch region before it
-// reads it, so the contents left by an earlier call never matter.
+// enough for frames up to 256 x 256).  Host code may not use its name as an
+// address, so each call looks the address up with cudaGetSymbolAddress (with
+// the caller's device current; a lookup allocates nothing once the array is
+// resident).  The first call on a device does the set-up: the lookup makes
+// the CUDA runtime load this library's module and place the array on the
+// device (CUDA loads modules lazily by default, so this is where the array's
+// memory is taken), the FFT twiddle tables are copied into it, and one
+// 16 x 16 warm-up shift runs every kernel the call uses, so that their
+// modules are loaded too.  That first call therefore allocates and must come
+// at start-up, before any stream capture; later calls allocate nothing.  A
+// device reset (cudaDeviceReset) discards the array: the next call sees a
+// new address and repeats the set-up, so it allocates again.
+//
+// All calls on a device share the array: two calls whose work overlaps on
+// the GPU race with each other and must be ordered by the caller (one
+// stream, or events).  Each call writes every scratch region before it reads
+// it, so the contents left by an earlier call never matter.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -48,12 +56,15 @@ constexpr size_t kOffQ = kOffM + align256((size_t)kMaxN * sizeof(float));       
 constexpr int kTw = 1 << (kTwLog - 1);
 constexpr size_t kOffTw = kOffQ + 256;                                   // FP32 twiddles
 constexpr size_t kOffTwDf = kOffTw + align256(kTw * sizeof(float2));     // float-float twiddles
-constexpr size_t kScratchBytes = kOffTwDf + align256(kTw * sizeof(dfc));
+constexpr size_t kOffWarm = kOffTwDf + align256(kTw * sizeof(dfc));     // warm-up frame (16 x 16 doubles, zero)
+constexpr size_t kWarmN = 16;
+constexpr size_t kOffWarmOut = kOffWarm + align256(kWarmN * kWarmN * sizeof(double)); // warm-up shift
+constexpr size_t kScratchBytes = kOffWarmOut + 256;
 
 static __device__ __align__(256) unsigned char g_xcorr_scratch[kScratchBytes];
 
 std::mutex g_mu;
-std::vector<unsigned char*> g_base; // per device: address of g_xcorr_scratch, null until set up
+std::vector<unsigned char*> g_base; // per device: the array's address when it was set up
 
 int fail(int code, const std::string& m)
 {
@@ -61,18 +72,25 @@ int fail(int code, const std::string& m)
     return code;
 }
 
-// Once per device, with that device current: look up the array's device
-// address and fill the twiddle tables.
-int setup(int dev, unsigned char** base)
+bool pow2_in(long v);
+int ilog2i(long v);
+cudaError_t run_shift(unsigned char* base, const double* ref, const double* frame, long ncols, long nrows, int* shift,
+                      cudaStream_t st);
+
+// With the caller's device current: look up the array's device address and,
+// when it is new for this device (first call, or after a device reset), fill
+// the twiddle tables and run one warm-up shift on a zero 16 x 16 frame held
+// in the array, which loads every kernel this entry point launches.
+int setup(int dev, cudaStream_t st, unsigned char** base)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     if ((int)g_base.size() <= dev)
         g_base.resize(dev + 1, nullptr);
-    if (!g_base[dev]) {
-        unsigned char* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_xcorr_scratch);
-        if (e != cudaSuccess)
-            return fail(SMIP_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    unsigned char* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&p), g_xcorr_scratch);
+    if (e != cudaSuccess)
+        return fail(SMIP_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    if (g_base[dev] != p) {
         std::vector<float2> t32(kTw);
         std::vector<dfc> tdf(kTw);
         for (int k = 0; k < kTw; ++k) {
@@ -87,9 +105,15 @@ int setup(int dev, unsigned char** base)
             e = cudaMemcpy(p + kOffTwDf, tdf.data(), sizeof(dfc) * kTw, cudaMemcpyHostToDevice);
         if (e != cudaSuccess)
             return fail(SMIP_E_CUDA, std::string("twiddle upload: ") + cudaGetErrorString(e));
+        const double* warm = reinterpret_cast<const double*>(p + kOffWarm);
+        e = cudaMemsetAsync(p + kOffWarm, 0, kWarmN * kWarmN * sizeof(double), st);
+        if (e == cudaSuccess)
+            e = run_shift(p, warm, warm, kWarmN, kWarmN, reinterpret_cast<int*>(p + kOffWarmOut), st);
+        if (e != cudaSuccess)
+            return fail(SMIP_E_CUDA, std::string("warm-up shift: ") + cudaGetErrorString(e));
         g_base[dev] = p;
     }
-    *base = g_base[dev];
+    *base = p;
     return SMIP_OK;
 }
 
@@ -103,23 +127,10 @@ int ilog2i(long v)
     return l;
 }
 
-} // namespace
-
-extern "C" int smip_xcorr_displacement_noalloc(const double* ref, const double* frame, long ncols, long nrows,
-                                               int* shift, void* stream)
+// The shift's kernels on stream st, every intermediate inside the array at base.
+cudaError_t run_shift(unsigned char* base, const double* ref, const double* frame, long ncols, long nrows, int* shift,
+                      cudaStream_t st)
 {
-    if (!ref || !frame || !shift)
-        return fail(SMIP_E_INVALID_ARGUMENT, "null device pointer");
-    if (!pow2_in(ncols) || !pow2_in(nrows))
-        return fail(SMIP_E_UNSUPPORTED, "smip_xcorr_displacement_noalloc: ncols and nrows must be powers of two in "
-                                        "[16, 256] (the fixed scratch array holds frames up to 256 x 256)");
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess)
-        return fail(SMIP_E_CUDA, "cudaGetDevice failed");
-    unsigned char* base = nullptr;
-    int rc = setup(dev, &base);
-    if (rc)
-        return rc;
     Geometry g {};
     g.W = (int)ncols;
     g.H = (int)nrows;
@@ -137,7 +148,6 @@ extern "C" int smip_xcorr_displacement_noalloc(const double* ref, const double* 
     double* refsq = reinterpret_cast<double*>(base + kOffQ);
     const float2* tw = reinterpret_cast<const float2*>(base + kOffTw);
     const dfc* twdf = reinterpret_cast<const dfc*>(base + kOffTwDf);
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     const long long n = (long long)ncols * nrows;
     cudaError_t e = launch_sumsq(SMIP_F64, ref, n, refsq, st);
     if (e == cudaSuccess) e = launch_row_pass(SMIP_F64, ref, n, 1, g, Gt, twdf, st);
@@ -146,6 +156,27 @@ extern "C" int smip_xcorr_displacement_noalloc(const double* ref, const double* 
     if (e == cudaSuccess) e = launch_col_pass(0, Gt + half, S, R, nullptr, T, Pp, 1, 16, 0, g, twdf, tw, st);
     if (e == cudaSuccess) e = launch_xcorr_rows(T, corr, rowmax, 1, g, tw, st);
     if (e == cudaSuccess) e = launch_xcorr_shift(SMIP_F64, corr, rowmax, frame, n, ref, refsq, 1, 0, g, shift, st);
+    return e;
+}
+
+} // namespace
+
+extern "C" int smip_xcorr_displacement_noalloc(const double* ref, const double* frame, long ncols, long nrows,
+                                               int* shift, void* stream)
+{
+    if (!ref || !frame || !shift)
+        return fail(SMIP_E_INVALID_ARGUMENT, "null device pointer");
+    if (!pow2_in(ncols) || !pow2_in(nrows))
+        return fail(SMIP_E_UNSUPPORTED, "smip_xcorr_displacement_noalloc: ncols and nrows must be powers of two in "
+                                        "[16, 256] (the fixed scratch array holds frames up to 256 x 256)");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return fail(SMIP_E_CUDA, "cudaGetDevice failed");
+    unsigned char* base = nullptr;
+    int rc = setup(dev, static_cast<cudaStream_t>(stream), &base);
+    if (rc)
+        return rc;
+    cudaError_t e = run_shift(base, ref, frame, ncols, nrows, shift, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess)
         return fail(SMIP_E_CUDA, cudaGetErrorString(e));
     return SMIP_OK;

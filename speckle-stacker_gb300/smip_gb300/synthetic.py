@@ -166,9 +166,20 @@ def _peak_norm(spec: StackSpec) -> float:
     return _PEAK_CACHE[key]
 
 
-def make_stack(spec: StackSpec, start: int = 0, count: int | None = None) -> np.ndarray:
-    """Frames [start, start+count) as an (count, n, n) array."""
+def make_stack(spec: StackSpec, start: int = 0, count: int | None = None, procs: int = 1) -> np.ndarray:
+    """Frames [start, start+count) as an (count, n, n) array.
+
+    procs > 1 generates chunks in a pool of fresh ("spawn") processes, which
+    is safe after CUDA has been initialised in this process; the frames are
+    the same for any chunking."""
     count = spec.nframes - start if count is None else count
+    if procs > 1 and count >= 2 * procs:
+        import multiprocessing as mp
+
+        chunk = (count + procs - 1) // procs
+        jobs = [(spec, start + s, min(chunk, count - s)) for s in range(0, count, chunk)]
+        with mp.get_context("spawn").Pool(len(jobs)) as pool:
+            return np.concatenate(pool.starmap(make_stack, jobs))
     obj_ft = _fft2(make_object(spec))
     out = np.empty((count, spec.n, spec.n), spec.np_dtype)
     for k in range(count):

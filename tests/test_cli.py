@@ -103,7 +103,7 @@ def test_cpp_layer_builds(tmp_path):
 
 
 @pytest.mark.gpu
-def test_cli_matches_binding(smip, tmp_path):
+def test_cli_matches_binding(smip, oracle, tmp_path):
     """smip-cli -b 20 -p 40 -n 10 on a 12-frame u8 stack: bispectrum.dat and every
     PNG equal what the binding gives for the same frames (default depth 20)."""
     _need_cli()
@@ -142,9 +142,20 @@ def test_cli_matches_binding(smip, tmp_path):
         got = read_png16(tmp_path / name)
         assert got.shape == e.shape
         assert np.abs(got.astype(np.int64) - e.astype(np.int64)).max() <= 1, name
-    for name in ("sum_image_falsecolor.png", "phases_falsecolor.png", "phasecons.png", "powerspec_falsecolor.png",
-                 "reco_image_falsecolor.png"):
-        assert read_png16(tmp_path / name).shape == (n, n, 3)
+    # false colour: the oracle's mapToColor (videoio.h:178-206) in Array2Mat's
+    # pixel order (videoio.h:137-146) of the same values
+    colour = {
+        "sum_image_falsecolor.png": (np.abs(sm / 255.0), False),
+        "phases_falsecolor.png": ((np.angle(ph * win) + np.pi) / (2 * np.pi), True),
+        "phasecons.png": (cons, True),
+        "powerspec_falsecolor.png": (np.abs(pw / (np.abs(pw).max() / 1000.0)), True),
+        "reco_image_falsecolor.png": (np.abs(img), True),
+    }
+    for name, (vals, signed) in colour.items():
+        e = oracle.map_to_color(oracle.array2mat_order(vals, signed))
+        got = read_png16(tmp_path / name)
+        assert got.shape == (n, n, 3), name
+        assert np.abs(got.astype(np.int64) - e.astype(np.int64)).max() <= 1, name
 
 
 @pytest.mark.gpu

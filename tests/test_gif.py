@@ -177,7 +177,9 @@ def test_reference_testdata_gif_decodes(gif_check, tmp_path):
     """The reference's own sample stack (data/testdata.gif, read by smip-cli
     through OpenCV): 40 frames of 128x128 decode to a speckle cloud brighter
     in the centre than at the edges."""
-    ref = "/root/reference/data/testdata.gif"
+    from oracle import REFERENCE
+
+    ref = os.path.join(REFERENCE, "data", "testdata.gif")
     if not os.path.exists(ref):
         pytest.skip("reference data not present")
     got = decode(gif_check, ref, tmp_path)
@@ -246,7 +248,9 @@ def test_reference_example_matches_published_images(gif_check, oracle, tmp_path)
     beside the GIF.  Those images were made by OpenCV's GIF reader, not this
     decoder, so they are compared by correlation: the reconstruction agrees at
     ncc 0.991, the shift-and-add sum at 0.984 once offset by one pixel in x."""
-    d = "/root/reference/data/hu940ani"
+    from oracle import REFERENCE
+
+    d = os.path.join(REFERENCE, "data", "hu940ani")
     if not os.path.exists(os.path.join(d, "hu940ani.gif")):
         pytest.skip("reference data not present")
     frames = decode(gif_check, os.path.join(d, "hu940ani.gif"), tmp_path)

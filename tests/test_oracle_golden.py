@@ -131,3 +131,31 @@ def test_accumulate_threads_invariant(oracle):
     oracle.accumulate(a, F, 8, nthreads=1)
     oracle.accumulate(b, F, 8, nthreads=5)
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_map_to_color_known_values(oracle):
+    """mapToColor<uint16_t> (videoio.h:178-206) at its band edges and inside
+    each band, worked out from the formula in double arithmetic and truncated
+    as static_cast<uint16_t> does: value -> (r, g, b)."""
+    M = 65535
+    cases = {
+        -0.5: (0, 0, 0), 0.0: (0, 0, 0), 0.1: (0, 0, 26214),          # 65535 * 0.4 truncated
+        0.25: (0, 0, M), 0.3: (0, 13106, 52428),                      # 4*0.3-1 = 0.19999.. -> 13106.99..
+        0.5: (0, M, 0), 0.6: (26213, 39321, 0),                        # 4*0.6-2 = 0.39999.. -> 26213.99..
+        0.75: (M, 0, 0), 0.9: (M, 0, 39321),                           # 4*0.9-3 = 0.60000..1 -> 39321.00..
+        1.0: (M, 0, M), 7.0: (M, 0, M), float("nan"): (0, 0, 0),
+    }
+    v = np.array(list(cases.keys()))
+    got = oracle.map_to_color(v)
+    for k, (value, exp) in enumerate(cases.items()):
+        assert tuple(int(x) for x in got[k]) == exp, (value, got[k], exp)
+
+
+def test_array2mat_order(oracle):
+    """Array2Mat with signed_symmetry shows element (x - n/2, y - n/2) at
+    pixel (x, y): an fftshift for even sizes; the identity without it."""
+    a = np.arange(6 * 8, dtype=float).reshape(6, 8)
+    assert np.array_equal(oracle.array2mat_order(a, True), np.fft.fftshift(a))
+    assert np.array_equal(oracle.array2mat_order(a, False), a)
+    b = np.arange(5 * 7, dtype=float).reshape(5, 7)   # odd sizes: min index -(n/2)
+    assert np.array_equal(oracle.array2mat_order(b, True), np.roll(b, (2, 3), axis=(0, 1)))
