@@ -16,8 +16,8 @@
  *   - complex values are interleaved (re, im): complex<float> bispectrum
  *     (include/types.h:33), complex<double> phases/images (types.h:32).
  *   - the bispectrum is the reference's packed half-space array, base_size =
- *     (ncols/2+1)(nrows+1)(d/2+1)(d+1) elements, d = bdepth rounded down to
- *     even (include/bispectrum.h:203-220, 324-349).
+ *     (ncols/2+1)((nrows/2)*2+1)(d/2+1)(d+1) elements, d = bdepth rounded
+ *     down to even (include/bispectrum.h:203-220, 324-349).
  *
  * Every call is asynchronous on the object's CUDA stream unless it returns
  * host data; host-data calls synchronise that stream first.
@@ -75,8 +75,10 @@ SMIP_GPU_API int smip_version(int* major, int* minor, int* patch);
  * (bispectrum.h:183-192, main.cpp:253) plus the accumulators above.
  * stream: a cudaStream_t to run on, or NULL for a stream owned by the stack.
  * batch_frames: frames per accumulation batch (0 = library default).
- * Supported: ncols, nrows powers of two in [16, 512]; bdepth/2*2 in [2, 64]
- * and < min(ncols, nrows). */
+ * Supported: any ncols, nrows in [3, 1024] (powers of two in [16, 512] run
+ * radix-2 transforms, every other size mixed-radix ones, as FFTW plans any
+ * size for the reference, main.cpp:256-259); bdepth/2*2 in [2, 64] and
+ * < min(ncols, nrows). */
 SMIP_GPU_API int smip_stack_create(smip_stack_t* out, int device, long ncols, long nrows,
                                    long bdepth, void* stream, long batch_frames);
 SMIP_GPU_API int smip_stack_destroy(smip_stack_t s);

@@ -18,7 +18,7 @@
 // help text describes: -r idx makes frame idx the cross-correlation reference (it
 // is accumulated first, then the others in order); -k l:t and -s w:h crop
 // every frame to that box before ingest (the box must lie inside the frame;
-// its size follows the stack's power-of-two rule); --no-calcsum leaves out the
+// any size the stack takes, 3 to 1024 per axis); --no-calcsum leaves out the
 // sum images; --no-specklemasking leaves out bispectrum.dat, the phase
 // reconstruction and the images made from it.  -f (follow) is not parsed by
 // the reference (getopt prints the usage) and is not here either.

@@ -98,6 +98,7 @@ struct BispecArgs {
     int* err;
     int nframes;
     int H, hw;
+    int bs1;      // packed extent of u_y: (H/2)*2 + 1
     int D;        // the stack's depth (even, <= DE): packed layout and stored elements
     int nchm;     // main chunks per (a0, j tile): ceil((D/2) / RPC)
     int njt;      // j tiles: ceil(H / JT)
@@ -200,6 +201,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
     }
     __syncthreads();
     const int half_h = p.H / 2;
+    const int jend = p.H - half_h; // u_y in [-(H/2), jend)
     const int nf = p.nframes;
     // this CTA's unit: tile blockIdx.x whole, or (split unit s = blockIdx.x -
     // nfull) part s % P of tile nfull + s / P, frames [part*nf/P, (part+1)*nf/P)
@@ -283,7 +285,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
         // A warp whose row has u + v outside the spectrum (every F(u+v) zero),
         // or whose row or j block lies outside the stack's layout, only keeps
         // the ring moving: its sums would be zero or unused.
-        const bool live = a0 < p.hw && jw < half_h && a0 + a2 < p.hw && (EXACT || a2 <= hd);
+        const bool live = a0 < p.hw && jw < jend && a0 + a2 < p.hw && (EXACT || a2 <= hd);
 
         float2 acc[8][Cf::TLW];
 #pragma unroll
@@ -416,12 +418,11 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
             // Kahan-compensated add of the batch partial into (B, C); within a
             // j step every load is issued before the first store (B and C never
             // alias).
-            const int H = p.H;
             const int rowE = (hd + 1) * (D + 1);
-            float2* __restrict__ Bt = p.B + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (D + 1);
-            float2* __restrict__ Ct = p.C + ((long long)a0 * (H + 1)) * rowE + (long long)a2 * (D + 1);
+            float2* __restrict__ Bt = p.B + ((long long)a0 * p.bs1) * rowE + (long long)a2 * (D + 1);
+            float2* __restrict__ Ct = p.C + ((long long)a0 * p.bs1) * rowE + (long long)a2 * (D + 1);
             auto off = [&](int j, int l) {
-                const int a1 = j >= 0 ? j : j + H + 1;
+                const int a1 = j >= 0 ? j : j + p.bs1;
                 const int a3 = l >= 0 ? l : l + D + 1;
                 return a1 * rowE + a3;
             };
@@ -432,8 +433,8 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
                 c.y = (ty - b.y) - yy;
                 b = make_float2(tx, ty);
             };
-            // a tile may reach past j = H/2 - 1 when H < JT: those sums are zero and not stored
-            const bool has_e = edge && jw + lane < half_h && DE == D;
+            // a tile may reach past the last u_y when H < JT: those sums are zero and not stored
+            const bool has_e = edge && jw + lane < jend && DE == D;
             const int oe = off(jw + lane, DE / 2);
             float2 be = make_float2(0.f, 0.f), ce = be;
             if (has_e) {
@@ -443,7 +444,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
 #pragma unroll
             for (int a = 0; a < 8; ++a) { // one j at a time keeps the register count down
                 const int j = jw + jg + 4 * a;
-                if (j < half_h) {
+                if (j < jend) {
                     int o[Cf::TLW];
                     float2 bv[Cf::TLW], cvv[Cf::TLW];
                     bool st[Cf::TLW];
@@ -503,15 +504,16 @@ static EncodeTiledFn get_encode()
     return fn;
 }
 
-// S viewed as UINT64 (one complex<float> per element) [nframes][hw][H];
-// box = {bcols, brows, nfb frames}.
+// S viewed as UINT64 (one complex<float> per element) [nframes][hw][Hs], H
+// columns used (Hs = H rounded up to even keeps the strides multiples of 16
+// bytes); box = {bcols, brows, nfb frames}.
 static bool make_map(CUtensorMap* m, const float2* S, int nframes, const Geometry& g, int bcols, int brows, int nfb)
 {
     EncodeTiledFn enc = get_encode();
     if (!enc)
         return false;
     const cuuint64_t dims[3] = { (cuuint64_t)g.H, (cuuint64_t)g.hw, (cuuint64_t)nframes };
-    const cuuint64_t strides[2] = { (cuuint64_t)g.H * 8, (cuuint64_t)g.H * 8 * g.hw };
+    const cuuint64_t strides[2] = { (cuuint64_t)g.Hs * 8, (cuuint64_t)g.Hs * 8 * g.hw };
     const cuuint32_t box[3] = { (cuuint32_t)bcols, (cuuint32_t)brows, (cuuint32_t)nfb };
     const cuuint32_t es[3] = { 1, 1, 1 };
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<float2*>(S), dims, strides, box, es,
@@ -540,6 +542,7 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
     a.nframes = L.nframes;
     a.H = g.H;
     a.hw = g.hw;
+    a.bs1 = g.bs1;
     a.D = g.De;
     a.nchm = (g.De / 2 + Cf::RPC - 1) / Cf::RPC;
     a.njt = (g.H + Cf::JT - 1) / Cf::JT;

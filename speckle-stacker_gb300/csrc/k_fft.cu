@@ -305,7 +305,8 @@ __global__ void __launch_bounds__(256) xcorr_rows_kernel(const float2* __restric
 
 // ----------------------------------------------------- spectrum import
 // FFT-order complex<double> spectra (ncols x nrows) -> S layout (float2).
-__global__ void import_spectra_kernel(const double2* __restrict__ in, int nframes, int W, int H, int hw,
+// S rows have pitch Hs >= H.
+__global__ void import_spectra_kernel(const double2* __restrict__ in, int nframes, int W, int H, int Hs, int hw,
                                       float2* __restrict__ S)
 {
     const long long per = (long long)hw * H;
@@ -314,10 +315,11 @@ __global__ void import_spectra_kernel(const double2* __restrict__ in, int nframe
         const long long f = i / per;
         const int rem = (int)(i - f * per);
         const int a = rem / H, c = rem - a * H;
-        const int x = (W - a) & (W - 1);
-        const int y = (c + H / 2) & (H - 1);
+        const int x = a == 0 ? 0 : W - a;   // x = -a
+        int y = c + (H - H / 2);            // y = c - H/2, wrapped
+        y -= y >= H ? H : 0;
         const double2 v = in[f * (long long)W * H + (long long)y * W + x];
-        S[i] = make_float2((float)v.x, (float)v.y);
+        S[(f * hw + a) * (long long)Hs + c] = make_float2((float)v.x, (float)v.y);
     }
 }
 
@@ -416,7 +418,7 @@ cudaError_t launch_import_spectra(const double* spectra, int nframes, const Geom
 {
     const long long n = (long long)g.hw * g.H * nframes;
     import_spectra_kernel<<<grid_for(n, 256), 256, 0, st>>>(reinterpret_cast<const double2*>(spectra), nframes, g.W,
-                                                             g.H, g.hw, S);
+                                                             g.H, g.Hs, g.hw, S);
     note_launches(1);
     return cudaGetLastError();
 }

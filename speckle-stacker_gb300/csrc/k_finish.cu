@@ -9,7 +9,9 @@
 
 namespace smip_gpu {
 
-__device__ __forceinline__ int signed_idx(int x, int n) { return x < n / 2 ? x : x - n; }
+// FFT-order index x -> the signed index of Array2's range [-(n/2), n - n/2 - 1]
+// (include/array2.h:310-339); for odd n the upper half is one longer.
+__device__ __forceinline__ int signed_idx(int x, int n) { return x < n - n / 2 ? x : x - n; }
 
 // power at FFT-order (x, y) from the u_x <= 0 half plane P[a][c]
 __device__ __forceinline__ double power_at(const double* Ph, int sx, int sy, int H)
@@ -20,7 +22,9 @@ __device__ __forceinline__ double power_at(const double* Ph, int sx, int sy, int
         c = sy + H / 2;
     } else { // P(x, y) = P(-x, -y)
         a = sx;
-        c = (H / 2 - sy) & (H - 1);
+        c = H / 2 - sy; // y = -sy, wrapped into [-(H/2), H - 1 - H/2]
+        if (c >= H)
+            c -= H;
     }
     return Ph[(long long)a * H + c];
 }
@@ -114,20 +118,28 @@ __global__ void scale_kernel(double2* __restrict__ Z, int n, const double* __res
 static int grid_n(int n) { return (n + 255) / 256 < 2048 ? (n + 255) / 256 : 2048; }
 
 cudaError_t launch_finish(const double* Phalf, double pnorm, const double2* phases, double aperture, const Geometry& g,
-                          double2* Z, double* power_full, double* maxbuf, const double2* tw64, cudaStream_t st)
+                          double2* Z, double* power_full, double* maxbuf, const double2* tw64, cudaStream_t st,
+                          const double2* twW64, const double2* twH64)
 {
     const int n = g.W * g.H;
     const double trigarg = 6.283185307179586476925286766559 / aperture;
     finish_build_kernel<<<grid_n(n), 256, 0, st>>>(Phalf, pnorm, phases, trigarg, g.W, g.H, Z, power_full); note_launches(1);
-    const size_t smem = sizeof(double2) * ((1 << (kTwLog - 1)) + 4 * (size_t)(g.W > g.H ? g.W : g.H));
-    // the limit is the largest frame's, so that concurrent launches of other shapes never lower it
-    const size_t smem_max = sizeof(double2) * ((1 << (kTwLog - 1)) + 4 * (size_t)(1 << kMaxLog));
-    cudaError_t e = cudaFuncSetAttribute(fft_lines_d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
-    if (e != cudaSuccess)
-        return e;
-    // FFTW_BACKWARD over rows (x) then columns (y)
-    fft_lines_d_kernel<<<(g.H + 3) / 4, 256, smem, st>>>(Z, g.logW, g.H, g.W, 1, +1, tw64); note_launches(1);
-    fft_lines_d_kernel<<<(g.W + 3) / 4, 256, smem, st>>>(Z, g.logH, g.W, 1, g.W, +1, tw64); note_launches(1);
+    cudaError_t e = cudaSuccess;
+    if (g.generic) { // FFTW_BACKWARD over rows (x) then columns (y), mixed radix
+        if ((e = launch_gen_lines_d(Z, g.pW, g.H, g.W, 1, +1, twW64, st)) != cudaSuccess
+            || (e = launch_gen_lines_d(Z, g.pH, g.W, 1, g.W, +1, twH64, st)) != cudaSuccess)
+            return e;
+    } else {
+        const size_t smem = sizeof(double2) * ((1 << (kTwLog - 1)) + 4 * (size_t)(g.W > g.H ? g.W : g.H));
+        // the limit is the largest frame's, so that concurrent launches of other shapes never lower it
+        const size_t smem_max = sizeof(double2) * ((1 << (kTwLog - 1)) + 4 * (size_t)(1 << kMaxLog));
+        e = cudaFuncSetAttribute(fft_lines_d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+        if (e != cudaSuccess)
+            return e;
+        // FFTW_BACKWARD over rows (x) then columns (y)
+        fft_lines_d_kernel<<<(g.H + 3) / 4, 256, smem, st>>>(Z, g.logW, g.H, g.W, 1, +1, tw64); note_launches(1);
+        fft_lines_d_kernel<<<(g.W + 3) / 4, 256, smem, st>>>(Z, g.logH, g.W, 1, g.W, +1, tw64); note_launches(1);
+    }
     if ((e = cudaMemsetAsync(maxbuf, 0, sizeof(double), st)) != cudaSuccess)
         return e;
     max_abs_kernel<<<(n + 255) / 256 < 256 ? (n + 255) / 256 : 256, 256, 0, st>>>(Z, n, maxbuf); note_launches(1);

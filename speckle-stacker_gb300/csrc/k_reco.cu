@@ -731,7 +731,7 @@ cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int
     // function; a launch of another shape must never lower it under this one);
     // the static shared memory (ring, phase cache) counts against it too
     const size_t smem_max = (sizeof(float2) + sizeof(int2)) * 65 * 65
-                            + sizeof(unsigned int) * (((size_t)1 << (2 * kMaxLog)) / 32);
+                            + sizeof(unsigned int) * (((size_t)kMaxSide * kMaxSide + 31) / 32);
     cudaError_t e = cudaFuncSetAttribute(phase_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     if (e != cudaSuccess)
         return e;

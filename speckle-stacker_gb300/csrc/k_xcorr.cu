@@ -11,7 +11,8 @@
 // u8/u16 frames, FP64 for float frames -- and the best exact value wins, ties
 // to the lowest linear index (std::max_element's first maximum).  The bound
 // is 8 * 2^-24 * log2(W*H) * ||ref||_2 * ||frame||_2 * W*H, a few times the
-// worst-case error of an FP32 radix-2 FFT convolution.
+// worst-case error of an FP32 radix-2 FFT convolution (for mixed-radix
+// transforms the sum of the factors of W and H takes the place of log2(W*H)).
 #include <cstdint>
 
 #include "smip_dev.cuh"
@@ -55,16 +56,18 @@ template <> __device__ __forceinline__ unsigned long long mul_exact<unsigned lon
 constexpr int kMulti = 8; // candidates scored per sweep over the frame
 
 // Exact correlations sum_p ref(p) frame((p + s_c) mod (W, H)) of up to kMulti
-// candidate shifts s_c = cand[c] (row-major index) in one sweep: four
-// consecutive pixels per thread step, shifts and masks instead of divisions.
-// Results land in out[c] for every thread.
+// candidate shifts s_c = cand[c] (row-major index) in one sweep.  Frames whose
+// width is a power of two (logW >= 0) take four consecutive pixels per thread
+// step with shifts and masks instead of divisions; other widths (logW = -1)
+// one pixel per step with wrapped indices.  Results land in out[c] for every
+// thread.
 template <typename T>
-__device__ void exact_corr_multi(const T* __restrict__ ref, const T* __restrict__ fr, int logW, int H,
+__device__ void exact_corr_multi(const T* __restrict__ ref, const T* __restrict__ fr, int W, int logW, int H,
                                  const int* cand, int k, typename ExactAcc<T>::type* out,
                                  typename ExactAcc<T>::type* red /* [kMulti][32] */)
 {
     using A = typename ExactAcc<T>::type;
-    const int W = 1 << logW, n = W * H;
+    const int n = W * H;
     A acc[kMulti];
 #pragma unroll
     for (int c = 0; c < kMulti; ++c)
@@ -73,11 +76,26 @@ __device__ void exact_corr_multi(const T* __restrict__ ref, const T* __restrict_
 #pragma unroll
     for (int c = 0; c < kMulti; ++c) {
         const int q = c < k ? cand[c] : 0;
-        sx[c] = q & (W - 1);
-        sy[c] = q >> logW;
+        sx[c] = q % W;
+        sy[c] = q / W;
     }
     const bool vec = (reinterpret_cast<uintptr_t>(ref) & 15) == 0;
-    for (int p = threadIdx.x * 4; p < n; p += blockDim.x * 4) {
+    if (logW < 0) {
+        for (int p = threadIdx.x; p < n; p += blockDim.x) {
+            const int y = p / W, x = p - y * W;
+            const T r = ref[p];
+#pragma unroll
+            for (int c = 0; c < kMulti; ++c) {
+                if (c < k) {
+                    int ys = y + sy[c], xs = x + sx[c];
+                    ys -= ys >= H ? H : 0;
+                    xs -= xs >= W ? W : 0;
+                    acc[c] += mul_exact<A>(r, fr[ys * W + xs]);
+                }
+            }
+        }
+    }
+    for (int p = threadIdx.x * 4; logW >= 0 && p < n; p += blockDim.x * 4) {
         const int x = p & (W - 1), y = p >> logW;
         T r4[4];
         if (vec && sizeof(T) == 1)
@@ -130,8 +148,8 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
                                                                      const float* __restrict__ rowmax,
                                                                      const T* __restrict__ frames, long long fstride,
                                                                      const T* __restrict__ ref, const double* ref_sq,
-                                                                     int first_is_frame0, int W, int H,
-                                                                     int* __restrict__ shifts)
+                                                                     int first_is_frame0, int W, int logW, int H,
+                                                                     double err_stages, int* __restrict__ shifts)
 {
     using A = typename ExactAcc<T>::type;
     __shared__ A redM[kMulti * 32];
@@ -191,7 +209,7 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
     mx = redF[0];
     for (int i = 1; i < (int)(blockDim.x >> 5); ++i)
         mx = fmaxf(mx, redF[i]);
-    const double tau = 8.0 * 5.9604644775390625e-08 * (double)(__ffs(n) - 1) * sqrt(*ref_sq * sq) * (double)n;
+    const double tau = 8.0 * 5.9604644775390625e-08 * err_stages * sqrt(*ref_sq * sq) * (double)n;
     const float thr = (float)((double)mx - tau);
 
     A best = 0;
@@ -200,7 +218,7 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
         for (int q0 = 0; q0 < nc; q0 += kMulti) {
             const int k = nc - q0 < kMulti ? nc - q0 : kMulti;
             A v[kMulti];
-            exact_corr_multi(ref, fr, __ffs(W) - 1, H, cand + q0, k, v, redM);
+            exact_corr_multi(ref, fr, W, logW, H, cand + q0, k, v, redM);
             for (int c = 0; c < k; ++c) {
                 const int p = cand[q0 + c];
                 if (best_idx < 0 || v[c] > best || (v[c] == best && p < best_idx)) {
@@ -220,17 +238,28 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
     for (int y = threadIdx.x >> 5; y < H; y += nwarps) {
         if (!(rm[y] >= thr))
             continue;
-        for (int x = lane * 4; x < W; x += 128) {
-            const int p = y * W + x;
-            const float4 cv = *reinterpret_cast<const float4*>(c + p);
-            const float e4[4] = { cv.x, cv.y, cv.z, cv.w };
+        if ((W & 3) == 0) {
+            for (int x = lane * 4; x < W; x += 128) {
+                const int p = y * W + x;
+                const float4 cv = *reinterpret_cast<const float4*>(c + p);
+                const float e4[4] = { cv.x, cv.y, cv.z, cv.w };
 #pragma unroll
-            for (int e = 0; e < 4; ++e)
-                if (e4[e] >= thr) {
+                for (int e = 0; e < 4; ++e)
+                    if (e4[e] >= thr) {
+                        const int slot = atomicAdd(&ncand, 1);
+                        if (slot < kMaxCand)
+                            cand[slot] = p + e;
+                    }
+            }
+        } else { // rows not 16-byte aligned
+            for (int x = lane; x < W; x += 32) {
+                const int p = y * W + x;
+                if (c[p] >= thr) {
                     const int slot = atomicAdd(&ncand, 1);
                     if (slot < kMaxCand)
-                        cand[slot] = p + e;
+                        cand[slot] = p;
                 }
+            }
         }
     }
     __syncthreads();
@@ -267,7 +296,7 @@ __global__ void __launch_bounds__(kShiftThreads) xcorr_shift_kernel(const float*
         flush();
     }
     if (threadIdx.x == 0) {
-        int sx = best_idx & (W - 1), sy = best_idx / W;
+        int sx = best_idx % W, sy = best_idx / W;
         sx -= (sx < (W + 1) / 2) ? 0 : W;
         sy -= (sy < (H + 1) / 2) ? 0 : H;
         shifts[2 * f] = sx;
@@ -298,7 +327,7 @@ __global__ void __launch_bounds__(256) saa_add_kernel(A* __restrict__ sum, const
     __syncthreads();
     const int n = W * H;
     for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        const int x = p & (W - 1), y = p / W;
+        const int y = p / W, x = p - y * W;
         A acc = kExact ? A(0) : sum[p];
         int f = fb;
         for (; f + 8 <= fe; f += 8) { // eight independent loads in flight, added in frame order
@@ -347,11 +376,21 @@ cudaError_t launch_xcorr_shift(int dtype, const float* corr, const float* rowmax
                                const void* ref, const double* ref_sq, int nframes, int first_is_frame0,
                                const Geometry& g, int* shifts, cudaStream_t st)
 {
+    // the correlation's FP32 error grows with the transforms' stages: log2(W H)
+    // radix-2 stages, or the sum of the mixed-radix factors (each pass a sum
+    // of that many terms) on the generic path
+    const int logW = g.generic ? -1 : g.logW;
+    double stages = g.logW + g.logH;
+    if (g.generic) {
+        stages = 0.0;
+        for (int k = 0; k < g.pW.nf; ++k) stages += g.pW.fac[k];
+        for (int k = 0; k < g.pH.nf; ++k) stages += g.pH.fac[k];
+    }
     switch (dtype) {
-    case 0: xcorr_shift_kernel<uint8_t><<<nframes, kShiftThreads, 0, st>>>(corr, rowmax, (const uint8_t*)frames, fstride, (const uint8_t*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
-    case 1: xcorr_shift_kernel<uint16_t><<<nframes, kShiftThreads, 0, st>>>(corr, rowmax, (const uint16_t*)frames, fstride, (const uint16_t*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
-    case 2: xcorr_shift_kernel<float><<<nframes, kShiftThreads, 0, st>>>(corr, rowmax, (const float*)frames, fstride, (const float*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
-    default: xcorr_shift_kernel<double><<<nframes, kShiftThreads, 0, st>>>(corr, rowmax, (const double*)frames, fstride, (const double*)ref, ref_sq, first_is_frame0, g.W, g.H, shifts); note_launches(1); break;
+    case 0: xcorr_shift_kernel<uint8_t><<<nframes, kShiftThreads, 0, st>>>(corr, rowmax, (const uint8_t*)frames, fstride, (const uint8_t*)ref, ref_sq, first_is_frame0, g.W, logW, g.H, stages, shifts); note_launches(1); break;
+    case 1: xcorr_shift_kernel<uint16_t><<<nframes, kShiftThreads, 0, st>>>(corr, rowmax, (const uint16_t*)frames, fstride, (const uint16_t*)ref, ref_sq, first_is_frame0, g.W, logW, g.H, stages, shifts); note_launches(1); break;
+    case 2: xcorr_shift_kernel<float><<<nframes, kShiftThreads, 0, st>>>(corr, rowmax, (const float*)frames, fstride, (const float*)ref, ref_sq, first_is_frame0, g.W, logW, g.H, stages, shifts); note_launches(1); break;
+    default: xcorr_shift_kernel<double><<<nframes, kShiftThreads, 0, st>>>(corr, rowmax, (const double*)frames, fstride, (const double*)ref, ref_sq, first_is_frame0, g.W, logW, g.H, stages, shifts); note_launches(1); break;
     }
     return cudaGetLastError();
 }

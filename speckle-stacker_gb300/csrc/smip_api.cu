@@ -145,8 +145,8 @@ size_t dtype_size(int dt)
 
 int make_geometry(long W, long H, long bdepth, Geometry* g)
 {
-    if (!pow2(W) || !pow2(H) || W < 16 || H < 16 || W > (1 << kMaxLog) || H > (1 << kMaxLog))
-        return fail(SMIP_E_UNSUPPORTED, "frame size must be a power of two in [16, 512] per axis");
+    if (W < 3 || H < 3 || W > kMaxSide || H > kMaxSide)
+        return fail(SMIP_E_UNSUPPORTED, "frame size must be in [3, 1024] per axis");
     const int De = (int)(bdepth / 2) * 2;
     if (bdepth < 0)
         return fail(SMIP_E_INVALID_ARGUMENT, "bdepth must be non-negative");
@@ -158,11 +158,49 @@ int make_geometry(long W, long H, long bdepth, Geometry* g)
     g->H = (int)H;
     g->logW = ilog2(W);
     g->logH = ilog2(H);
+    // radix-2 kernels for powers of two in [16, 512]; mixed radix otherwise
+    g->generic = !(pow2(W) && pow2(H) && W >= 16 && H >= 16 && W <= (1 << kMaxLog) && H <= (1 << kMaxLog));
     g->hw = (int)W / 2 + 1;
+    g->Hs = (int)H + (int)(H & 1);
+    g->bs1 = (int)(H / 2) * 2 + 1;
     g->De = De;
     g->E = (De / 2 + 1) * (De + 1);
-    g->base_size = (long long)g->hw * (H + 1) * g->E;
+    g->base_size = (long long)g->hw * g->bs1 * g->E;
+    g->pW = make_gen_plan((int)W);
+    g->pH = make_gen_plan((int)H);
     return SMIP_OK;
+}
+
+// Generic path: twiddle tables exp(-2 pi i k / L), k < L, in float-float,
+// FP32 and FP64.
+int make_gen_tw(int L, GenTw* t)
+{
+    std::vector<double2> t64(L);
+    std::vector<float2> t32(L);
+    std::vector<dfc> tdf(L);
+    for (int k = 0; k < L; ++k) {
+        const double a = 2.0 * M_PI * (double)k / (double)L;
+        t64[k] = make_double2(std::cos(a), -std::sin(a));
+        const float hx = (float)t64[k].x, hy = (float)t64[k].y;
+        t32[k] = make_float2(hx, hy);
+        tdf[k].h = t32[k];
+        tdf[k].l = make_float2((float)(t64[k].x - (double)hx), (float)(t64[k].y - (double)hy));
+    }
+    CUDA_TRY(cudaMalloc(&t->df, sizeof(dfc) * L));
+    CUDA_TRY(cudaMalloc(&t->f32, sizeof(float2) * L));
+    CUDA_TRY(cudaMalloc(&t->f64, sizeof(double2) * L));
+    CUDA_TRY(cudaMemcpy(t->df, tdf.data(), sizeof(dfc) * L, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(t->f32, t32.data(), sizeof(float2) * L, cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(t->f64, t64.data(), sizeof(double2) * L, cudaMemcpyHostToDevice));
+    return SMIP_OK;
+}
+
+void free_gen_tw(GenTw* t)
+{
+    if (t->df) cudaFree(t->df);
+    if (t->f32) cudaFree(t->f32);
+    if (t->f64) cudaFree(t->f64);
+    *t = GenTw();
 }
 
 // phasereco.cpp:17-36, the reference's own host arithmetic
@@ -440,6 +478,7 @@ struct smip_stack {
     double2* Z = nullptr;
     double* pfull = nullptr;
     double* maxbuf = nullptr;
+    GenTw twW, twH;               // generic path: twiddles of the row and column lengths
     // phase recovery and the final image: a high-priority stream
     cudaStream_t rst = nullptr;
     cudaEvent_t ev_reco = nullptr;
@@ -478,6 +517,8 @@ struct smip_stack {
         dfree(ref_sq); dfree(Gt); dfree(T); dfree(S); dfree(R); dfree(corr); dfree(rowmax); dfree(shifts); dfree(err);
         dfree(kscratch); dfree(ktile_cnt);
         dfree(Z); dfree(pfull); dfree(maxbuf);
+        free_gen_tw(&twW);
+        free_gen_tw(&twH);
         for (auto& e : ev_pool) {
             cudaEventDestroy(e.first);
             cudaEventDestroy(e.second);
@@ -504,7 +545,16 @@ struct smip_stack {
         CUDA_TRY(cudaMemsetAsync(sum, 0, 8 * frame_elems(), st));
         CUDA_TRY(cudaMalloc(&Gt, sizeof(dfc) * half_elems() * Bf));
         CUDA_TRY(cudaMalloc(&T, sizeof(float2) * half_elems() * Bf));
-        CUDA_TRY(cudaMalloc(&S, sizeof(float2) * half_elems() * Bf));
+        CUDA_TRY(cudaMalloc(&S, sizeof(float2) * (size_t)g.hw * g.Hs * Bf));
+        if (g.Hs != g.H) // the pitch's spare column is never written: keep it defined
+            CUDA_TRY(cudaMemsetAsync(S, 0, sizeof(float2) * (size_t)g.hw * g.Hs * Bf, st));
+        if (g.generic) {
+            int rc = make_gen_tw(g.W, &twW);
+            if (!rc)
+                rc = make_gen_tw(g.H, &twH);
+            if (rc)
+                return rc;
+        }
         CUDA_TRY(cudaMalloc(&R, sizeof(float2) * half_elems()));
         CUDA_TRY(cudaMalloc(&corr, sizeof(float) * frame_elems() * Bf));
         CUDA_TRY(cudaMalloc(&rowmax, sizeof(float) * g.H * Bf));
@@ -602,19 +652,35 @@ struct smip_stack {
                 CUDA_TRY(cudaMemcpyAsync(ref, zc ? zc : staging, dtype_size(dtype) * fe, cudaMemcpyDefault, q));
                 CUDA_TRY(launch_sumsq(dtype, ref, (long long)fe, ref_sq, q));
             }
-            if (zc) {
-                CUDA_TRY(launch_row_pass(dtype, zc, (long long)fe, n, g, Gt, ctx->twdf, q, staging));
-                CUDA_TRY(cudaEventRecord(ev_zc, q));
-                CUDA_TRY(cudaStreamWaitEvent(cst, ev_zc, 0));
+            if (g.generic) { // mixed-radix transforms (frame sizes other than powers of two in [16, 512])
+                if (zc) {
+                    CUDA_TRY(launch_gen_row_pass(dtype, zc, (long long)fe, n, g, Gt, twW.df, q, staging));
+                    CUDA_TRY(cudaEventRecord(ev_zc, q));
+                    CUDA_TRY(cudaStreamWaitEvent(cst, ev_zc, 0));
+                } else {
+                    CUDA_TRY(launch_gen_row_pass(dtype, staging, (long long)fe, n, g, Gt, twW.df, q));
+                }
+                if (first)
+                    CUDA_TRY(launch_gen_col_pass(1, Gt, S, R, R, T, Ppart, 1, fpc, 0, g, twH.df, twH.f32, q));
+                CUDA_TRY(launch_gen_col_pass(0, Gt, S, R, nullptr, T, Ppart, n, fpc, first ? 1 : 0, g, twH.df, twH.f32,
+                                             q));
+                CUDA_TRY(launch_power_reduce(P, Ppart, (n + fpc - 1) / fpc, g, q));
+                CUDA_TRY(launch_gen_xcorr_rows(T, corr, rowmax, n, g, twW.f32, q));
             } else {
-                CUDA_TRY(launch_row_pass(dtype, staging, (long long)fe, n, g, Gt, ctx->twdf, q));
+                if (zc) {
+                    CUDA_TRY(launch_row_pass(dtype, zc, (long long)fe, n, g, Gt, ctx->twdf, q, staging));
+                    CUDA_TRY(cudaEventRecord(ev_zc, q));
+                    CUDA_TRY(cudaStreamWaitEvent(cst, ev_zc, 0));
+                } else {
+                    CUDA_TRY(launch_row_pass(dtype, staging, (long long)fe, n, g, Gt, ctx->twdf, q));
+                }
+                if (first)
+                    CUDA_TRY(launch_col_pass(1, Gt, S, R, R, T, Ppart, 1, fpc, 0, g, ctx->twdf, ctx->tw32, q));
+                CUDA_TRY(launch_col_pass(0, Gt, S, R, nullptr, T, Ppart, n, fpc, first ? 1 : 0, g, ctx->twdf,
+                                         ctx->tw32, q));
+                CUDA_TRY(launch_power_reduce(P, Ppart, (n + fpc - 1) / fpc, g, q));
+                CUDA_TRY(launch_xcorr_rows(T, corr, rowmax, n, g, ctx->tw32, q));
             }
-            if (first)
-                CUDA_TRY(launch_col_pass(1, Gt, S, R, R, T, Ppart, 1, fpc, 0, g, ctx->twdf, ctx->tw32, q));
-            CUDA_TRY(launch_col_pass(0, Gt, S, R, nullptr, T, Ppart, n, fpc, first ? 1 : 0, g, ctx->twdf, ctx->tw32,
-                                     q));
-            CUDA_TRY(launch_power_reduce(P, Ppart, (n + fpc - 1) / fpc, g, q));
-            CUDA_TRY(launch_xcorr_rows(T, corr, rowmax, n, g, ctx->tw32, q));
             CUDA_TRY(launch_xcorr_shift(dtype, corr, rowmax, staging, (long long)fe, ref, ref_sq, n, first ? 1 : 0,
                                         g, shifts + 2 * first_index, q));
             CUDA_TRY(launch_saa_add(dtype, sum, staging, (long long)fe, n, first ? 1 : 0, shifts + 2 * first_index, g, q));
@@ -1244,7 +1310,8 @@ extern "C" int smip_stack_finish(smip_stack_t s, double R, double* image, double
         CUDA_TRY(cudaMalloc(&s->maxbuf, sizeof(double)));
     }
     const double pnorm = (double)((size_t)s->nframes * n);
-    CUDA_TRY(launch_finish(s->P, pnorm, s->reco.phases, 2.0 * R, s->g, s->Z, nullptr, s->maxbuf, s->ctx->tw64, s->rst));
+    CUDA_TRY(launch_finish(s->P, pnorm, s->reco.phases, 2.0 * R, s->g, s->Z, nullptr, s->maxbuf, s->ctx->tw64, s->rst,
+                           s->twW.f64, s->twH.f64));
     if ((rc = rejoin_stream(s)))
         return rc;
     if (image)
@@ -1607,7 +1674,9 @@ extern "C" int smip_xcorr_displacement(int device, const double* refimg, const d
     if (!refimg || !frame || !dx || !dy)
         return fail(SMIP_E_INVALID_ARGUMENT, "null argument");
     smip_stack_t s = nullptr;
-    int rc = smip_stack_create(&s, device, ncols, nrows, 8, nullptr, 16);
+    // the smallest depth the shape takes: only the correlation is used
+    const long depth = std::max(2L, std::min(8L, (std::min(ncols, nrows) - 1) / 2 * 2));
+    int rc = smip_stack_create(&s, device, ncols, nrows, depth, nullptr, 16);
     if (rc)
         return rc;
     const size_t n = (size_t)ncols * nrows;
@@ -1702,8 +1771,8 @@ extern "C" int smip_hann(int device, double* out, long xsize, long ysize, double
         return fail(SMIP_E_INVALID_ARGUMENT, "null output");
     if (!(aperture > 0.))
         return fail(SMIP_E_DOMAIN, "WindowFunction aperture size <= 0");
-    if (!pow2(xsize) || !pow2(ysize))
-        return fail(SMIP_E_UNSUPPORTED, "window size must be a power of two per axis");
+    if (xsize < 1 || ysize < 1)
+        return fail(SMIP_E_INVALID_ARGUMENT, "window size must be positive");
     CUDA_TRY(cudaSetDevice(device));
     double* d = nullptr;
     CUDA_TRY(cudaMalloc(&d, sizeof(double) * xsize * ysize));

@@ -16,24 +16,45 @@ enum : int {
     SMIP_DEV_ERR_OUT_OF_RANGE = 2, // Bispectrum::get_element would throw
 };
 
-constexpr int kMaxLog = 9;        // frames up to 512 x 512
+constexpr int kMaxLog = 9;        // radix-2 kernels: frames up to 512 x 512
 constexpr int kTwLog = kMaxLog;   // twiddle table for length 2^kTwLog
+constexpr int kMaxSide = 1024;    // any frame side up to this (mixed-radix kernels, k_fftg.cu)
+constexpr int kMaxFactors = 16;
+
+// Factorisation of one transform length for the mixed-radix kernels.
+struct GenPlan {
+    int L;
+    int nf;
+    int fac[kMaxFactors];
+};
+GenPlan make_gen_plan(int L);
 constexpr int kRowBlock = 16;     // rows per CTA in the row passes
 constexpr int kColLines = 8;      // frames per FFT pass in the column kernel
 
 // Geometry of one stack (all derived from ncols = W, nrows = H, depth).
 struct Geometry {
-    int W, H;         // frame size (powers of two)
-    int logW, logH;
+    int W, H;         // frame size
+    int logW, logH;   // radix-2 path: log2 of W and H
+    bool generic;     // W or H not a power of two in [16, 512]: mixed-radix kernels
     int hw;           // W/2 + 1: u_x half-plane rows a = -x in [0, W/2]
+    int Hs;           // row pitch of the spectra S (H rounded up to even: 16-byte TMA strides)
+    int bs1;          // packed bispectrum extent of u_y: (H/2)*2 + 1 (bispectrum.h:203-220)
     int De;           // bispectrum depth rounded down to even
     int E;            // packed elements per (u_x, u_y): (De/2+1)(De+1)
     long long base_size;
+    GenPlan pW, pH;   // generic path: factorisations of W and H
 };
+
 
 // float-float complex value hi + lo (forward-FFT intermediates, twiddles)
 struct dfc {
     float2 h, l;
+};
+// Twiddle tables of one transform length L (generic path): exp(-2 pi i k / L), k < L.
+struct GenTw {
+    dfc* df = nullptr;
+    float2* f32 = nullptr;
+    double2* f64 = nullptr;
 };
 
 // Every kernel launch site reports itself here (process-wide counter).
@@ -74,6 +95,20 @@ cudaError_t launch_xcorr_shift(int dtype, const float* corr, const float* rowmax
 // the stack's frame 0 enters with its sign (smip-cli/main.cpp:266).
 cudaError_t launch_saa_add(int dtype, void* sum, const void* frames, long long frame_stride_elems, int nframes,
                            int first_is_frame0, const int* shifts, const Geometry& g, cudaStream_t st);
+
+// Mixed-radix counterparts of the three launchers above for the generic path
+// (k_fftg.cu); same inputs and outputs, twiddles from the stack's GenTw tables.
+cudaError_t launch_gen_row_pass(int dtype, const void* frames, long long fstride, int nframes, const Geometry& g,
+                                dfc* Gt, const dfc* twW, cudaStream_t st, void* copy_out = nullptr);
+cudaError_t launch_gen_col_pass(int mode, const dfc* Gt, float2* S, const float2* Rbuf, float2* Rout, float2* T,
+                                double* Ppart, int nframes, int fpc, int skip_xcorr_frame0, const Geometry& g,
+                                const dfc* twH, const float2* twH32, cudaStream_t st);
+cudaError_t launch_gen_xcorr_rows(const float2* T, float* corr, float* rowmax, int nframes, const Geometry& g,
+                                  const float2* twW32, cudaStream_t st);
+// In-place FP64 transforms of nlines lines of length p.L (element stride es,
+// line stride ls); sign -1 forward, +1 inverse (unnormalised).
+cudaError_t launch_gen_lines_d(double2* data, const GenPlan& p, int nlines, long long ls, long long es, int sign,
+                               const double2* tw, cudaStream_t st);
 
 // FFT-order complex<double> spectra -> S layout (float2).
 cudaError_t launch_import_spectra(const double* spectra, int nframes, const Geometry& g, float2* S, cudaStream_t st);
@@ -140,7 +175,8 @@ cudaError_t launch_offset_probe(const Geometry& g, const int* idx, long long n, 
 // FFT, divide by max |.|.  Also writes the full-plane normalised power.
 cudaError_t launch_finish(const double* Phalf, double pnorm, const double2* phases, double aperture,
                           const Geometry& g, double2* Z, double* power_full, double* maxbuf, const double2* tw64,
-                          cudaStream_t st);
+                          cudaStream_t st,
+                          const double2* twW64 = nullptr, const double2* twH64 = nullptr);
 cudaError_t launch_power_full(const double* Phalf, double pnorm, const Geometry& g, double* power_full,
                               cudaStream_t st);
 cudaError_t launch_hann(double* out, int W, int H, double aperture, cudaStream_t st);

@@ -108,7 +108,7 @@ int main(int argc, char** argv)
     } catch (const std::domain_error&) {
     }
     try {
-        g::Stack bad(100, 64, 16);
+        g::Stack bad(2048, 64, 16); // frame sides above 1024 are refused
         return 6;
     } catch (const g::unsupported&) {
     }

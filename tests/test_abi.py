@@ -37,9 +37,11 @@ def test_next_reco_index_and_visits(smip):
         assert hashlib.sha256(v.astype(np.int32).tobytes()).hexdigest() == str(fx[f"r{R}_sha"])
 
 
-@pytest.mark.parametrize("shape", [(100, 128, 16), (128, 128, 66), (128, 128, 1), (128, 128, 128), (8, 8, 4),
-                                   (1024, 1024, 16), (16, 16, 16)])
+@pytest.mark.parametrize("shape", [(128, 128, 66), (128, 128, 1), (128, 128, 128), (4, 100, 4), (2, 64, 2),
+                                   (1025, 64, 8), (64, 2048, 8), (16, 16, 16)])
 def test_unsupported_shapes_rejected(smip, shape):
+    """Depths outside [2, 64] or not below the frame, and sides outside
+    [3, 1024], are refused before any device work."""
     with pytest.raises(smip.Unsupported):
         smip.Stack(*shape)
 
@@ -53,3 +55,7 @@ def test_base_size(smip):
     assert smip.bispec_base_size(256, 256, 32) == 18598833
     assert smip.bispec_base_size(512, 512, 48) == 161505225
     assert smip.bispec_base_size(128, 128, 33) == smip.bispec_base_size(128, 128, 32)
+    from oracle import bispec_desc
+
+    for W, H, D in ((99, 75, 14), (100, 100, 20), (640, 480, 16), (37, 64, 8)):  # any frame size
+        assert smip.bispec_base_size(W, H, D) == bispec_desc(W, H, D)["base_size"]

@@ -211,8 +211,9 @@ def test_cli_reads_animated_gif(smip, tmp_path):
 
 @pytest.mark.gpu
 def test_cli_apply_ignored(smip, tmp_path):
-    """--apply-ignored -r 3 -k 32:16 -s 64:64: frame 3 is the correlation
-    reference and every frame is cut to the 64x64 box at column 32, row 16;
+    """--apply-ignored -r 3 -k 32:16 -s 71:59: frame 3 is the correlation
+    reference and every frame is cut to the 71x59 box at column 32, row 16
+    (an odd size on both axes, as the reference's FFTW plans take);
     --no-calcsum drops the sum images, --no-specklemasking the bispectrum and
     everything made from it.  Outputs equal the binding on those frames."""
     _need_cli()
@@ -224,14 +225,14 @@ def test_cli_apply_ignored(smip, tmp_path):
     d1, d2 = tmp_path / "a", tmp_path / "b"
     d1.mkdir()
     d2.mkdir()
-    base = [CLI, "--apply-ignored", "-r", "3", "-k", "32:16", "-s", "64:64", "-b", "16", "-p", "20"]
+    base = [CLI, "--apply-ignored", "-r", "3", "-k", "32:16", "-s", "71:59", "-b", "16", "-p", "20"]
     r = subprocess.run(base + ["--no-calcsum", str(src)], capture_output=True, text=True, cwd=d1)
     assert r.returncode == 0, r.stderr
     r = subprocess.run(base + ["--no-specklemasking", str(src)], capture_output=True, text=True, cwd=d2)
     assert r.returncode == 0, r.stderr
     order = [3] + [i for i in range(12) if i != 3]
-    used = np.ascontiguousarray(frames[order][:, 16:80, 32:96])
-    with smip.Stack(64, 64, 16) as st:
+    used = np.ascontiguousarray(frames[order][:, 16:75, 32:103])
+    with smip.Stack(71, 59, 16) as st:
         st.push_frames(used)
         ref_dat = tmp_path / "ref.dat"
         st.save_bispectrum(str(ref_dat))
@@ -239,10 +240,10 @@ def test_cli_apply_ignored(smip, tmp_path):
         sm = st.sum()
     assert open(d1 / "bispectrum.dat", "rb").read() == open(ref_dat, "rb").read()
     assert not (d1 / "sum_image.png").exists() and not (d1 / "sum_image_falsecolor.png").exists()
-    exp = np.clip(np.roll(np.abs(img), (32, 32), axis=(0, 1)) * 65535.0, 0, 65535).astype(np.uint16)
+    exp = np.clip(np.roll(np.abs(img), (59 // 2, 71 // 2), axis=(0, 1)) * 65535.0, 0, 65535).astype(np.uint16)
     assert np.abs(read_png16(d1 / "reco_image.png").astype(np.int64) - exp).max() <= 1
     for name in ("bispectrum.dat", "reco_image.png", "phases.png", "phasecons.png"):
         assert not (d2 / name).exists(), name
     exp = np.clip(np.abs(sm / 255.0) * 65535.0, 0, 65535).astype(np.uint16)
     assert np.abs(read_png16(d2 / "sum_image.png").astype(np.int64) - exp).max() <= 1
-    assert read_png16(d2 / "powerspec.png").shape == (64, 64)
+    assert read_png16(d2 / "powerspec.png").shape == (59, 71)
