@@ -314,8 +314,8 @@ def serving_metrics(jobs):
                     "frames_per_s_ratio": s["frames_per_s"] / p["frames_per_s"],
                     "results_identical": serve.compare_results(res_s, res_p),
                     "peak_jobs_in_flight": eng.peak_active,
-                    "served_graph": sg, "frames_per_s_ratio_graph": sg["frames_per_s"] / p["frames_per_s"],
-                    "results_identical_graph": serve.compare_results(res_g, res_p),
+                    "served_multi": sg, "frames_per_s_ratio_multi": sg["frames_per_s"] / p["frames_per_s"],
+                    "results_identical_multi": serve.compare_results(res_g, res_p),
                     "served_rings": serve.summarize(*min(runs_r, key=lambda x: x[1]))}
         del eng, eng_g
     del keep

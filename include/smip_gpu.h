@@ -121,13 +121,17 @@ SMIP_GPU_API int smip_stack_reset(smip_stack_t s);
 SMIP_GPU_API int smip_stack_flush(smip_stack_t s);
 SMIP_GPU_API int smip_stack_sync(smip_stack_t s);
 
-/* Runs the pending (staged, not yet launched) frame batches of count stacks
- * as one CUDA graph: one branch per stack, the branches concurrent.  Stacks
- * without pending frames are skipped; all must live on one device and appear
- * once.  Later calls on each stack are ordered after the graph.  The results
- * are those of smip_stack_flush on each stack.  No counterpart in the
- * reference, which accumulates one stack per smip-cli run (main.cpp:281-312);
- * this is the graph-captured many-stack launch the serving loop uses. */
+/* Runs the pending (staged, not yet launched) frame batches of count stacks:
+ * each stack's per-frame kernels on its own stream, then the bispectrum work
+ * of all of them -- any frame sizes and depths -- as ONE persistent launch
+ * over a device work list of every stack's tiles, longest first.  That launch
+ * is a CUDA graph captured once (its stack records and work list are copied
+ * into device memory by the graph itself; it is captured again only when its
+ * buffers grow).  Stacks without pending frames are skipped; all must live on
+ * one device and appear once.  Later calls on each stack are ordered after
+ * the launch.  The results are bit-identical to smip_stack_flush on each
+ * stack.  No counterpart in the reference, which accumulates one stack per
+ * smip-cli run (main.cpp:281-312); the serving loop uses it. */
 SMIP_GPU_API int smip_batch_launch(smip_stack_t* stacks, long count);
 
 /* Diagnostic of the failure path: runs a kernel whose two waits (an mbarrier

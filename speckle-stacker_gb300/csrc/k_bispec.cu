@@ -50,6 +50,8 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <cstring>
+#include <vector>
 
 #include "smip_dev.cuh"
 
@@ -179,15 +181,19 @@ __device__ __forceinline__ void cmac(float2& acc, float2 a, float2 v, float2 w)
     acc.y = fmaf(ti, w.x, fmaf(-tr, w.y, acc.y));
 }
 
-// EXACT: the stack's depth is DE itself (compile-time layout); otherwise the
-// depth comes from the arguments (BispecArgs::D < DE).
+// One unit of work -- tile `unit` whole, or a frame part of a split tile --
+// by all threads of the block: ring set-up, the frame loop and the
+// Kahan-compensated epilogue.  EXACT: the stack's depth is DE itself
+// (compile-time layout); otherwise the depth comes from the arguments
+// (BispecArgs::D < DE).  Returns false when a bounded wait expired (the
+// error is recorded in p.err).  On return every copy this unit issued has
+// landed and the ring's barriers are invalidated, so the shared memory can
+// take the next unit.
 template <int DE, bool EXACT>
-__global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
-    bispec_accum_kernel(const __grid_constant__ CUtensorMap tmW, const __grid_constant__ CUtensorMap tmV,
-                        const __grid_constant__ CUtensorMap tmA, const BispecArgs p)
+__device__ __forceinline__ bool bispec_unit(unsigned char* smem, const CUtensorMap* tmW, const CUtensorMap* tmV,
+                                            const CUtensorMap* tmA, const BispecArgs& p, const int unit)
 {
     using Cf = BCfg<DE>;
-    extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + Cf::NS * Cf::STAGE);
     uint64_t* empty = full + Cf::NS;
     uint32_t* hi_issued = reinterpret_cast<uint32_t*>(empty + Cf::NS); // highest iteration issued + 1
@@ -203,10 +209,10 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
     const int half_h = p.H / 2;
     const int jend = p.H - half_h; // u_y in [-(H/2), jend)
     const int nf = p.nframes;
-    // this CTA's unit: tile blockIdx.x whole, or (split unit s = blockIdx.x -
+    // this CTA's unit: tile unit whole, or (split unit s = unit -
     // nfull) part s % P of tile nfull + s / P, frames [part*nf/P, (part+1)*nf/P)
-    const bool split_unit = (int)blockIdx.x >= p.nfull;
-    auto split_s = [&]() { return (int)blockIdx.x - p.nfull; };
+    const bool split_unit = (int)unit >= p.nfull;
+    auto split_s = [&]() { return (int)unit - p.nfull; };
     auto split_tile = [&]() { return p.nfull + split_s() / p.P; };
     auto split_f0 = [&]() { return (int)((long long)(split_s() % p.P) * nf / p.P); };
     auto split_f1 = [&]() { return (int)((long long)(split_s() % p.P + 1) * nf / p.P); };
@@ -227,13 +233,13 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
         unsigned char* st = smem + s * Cf::STAGE;
         if (!s_box[6]) {
             mbar_arrive_expect_tx(&full[s], Cf::FPS * (Cf::WBYTES + Cf::VBYTES + Cf::ABYTES));
-            tma_load_3d(st + Cf::WOFF, &tmW, s_box[0], s_box[1], f, &full[s]);
-            tma_load_3d(st + Cf::VOFF, &tmV, cv, s_box[2], f, &full[s]);
-            tma_load_3d(st + Cf::AOFF, &tmA, s_box[3], s_box[4], f, &full[s]);
+            tma_load_3d(st + Cf::WOFF, tmW, s_box[0], s_box[1], f, &full[s]);
+            tma_load_3d(st + Cf::VOFF, tmV, cv, s_box[2], f, &full[s]);
+            tma_load_3d(st + Cf::AOFF, tmA, s_box[3], s_box[4], f, &full[s]);
         } else {
             mbar_arrive_expect_tx(&full[s], Cf::FPS * (Cf::WBYTES + Cf::VBYTES));
-            tma_load_3d(st + Cf::WOFF, &tmW, s_box[0], s_box[1], f, &full[s]);
-            tma_load_3d(st + Cf::VOFF, &tmV, cv, s_box[2], f, &full[s]);
+            tma_load_3d(st + Cf::WOFF, tmW, s_box[0], s_box[1], f, &full[s]);
+            tma_load_3d(st + Cf::VOFF, tmV, cv, s_box[2], f, &full[s]);
         }
     };
 
@@ -241,7 +247,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
     // that finishes iteration r with r % WARPS == warp issues r + NS - LAG.
     constexpr uint32_t kAhead = Cf::NS - Cf::LAG;
     if (threadIdx.x == 0) {
-        const TileInfo ti = decode_tile<DE>(split_unit ? split_tile() : (int)blockIdx.x, p);
+        const TileInfo ti = decode_tile<DE>(split_unit ? split_tile() : (int)unit, p);
         s_box[0] = (ti.j0 + half_h - DE / 2) & ~1;
         s_box[1] = ti.row0 ? ti.a0 : ti.a0 + 1 + ti.c * Cf::RPC;
         s_box[2] = ti.row0 ? 0 : 1 + ti.c * Cf::RPC;
@@ -269,7 +275,7 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
     __shared__ int s_last; // this CTA completes its split tile
     for (int k = 0; k < 1 && ok; ++k) {
         const int nfu = (int)total; // frames of this unit
-        const TileInfo ti = decode_tile<DE>(split_unit ? split_tile() : (int)blockIdx.x, p);
+        const TileInfo ti = decode_tile<DE>(split_unit ? split_tile() : (int)unit, p);
         const int a0 = ti.row0 ? ti.a0 + wr : ti.a0;
         const int a2 = ti.row0 ? 0 : 1 + ti.c * Cf::RPC + wr;
         const int vrow = ti.row0 ? 0 : wr;
@@ -483,7 +489,20 @@ __global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
         for (uint32_t q = hi > (uint32_t)Cf::NS ? hi - Cf::NS : 0; q < hi; ++q)
             if (!mbar_wait_bounded(&full[q % Cf::NS], (q / Cf::NS) & 1, kWaitNs / 4))
                 break;
+        for (int q = 0; q < 2 * Cf::NS; ++q) // the next unit initialises them afresh
+            mbar_inval(&full[q]);
     }
+    __syncthreads();
+    return ok;
+}
+
+template <int DE, bool EXACT>
+__global__ void __launch_bounds__(BCfg<DE>::THREADS, kCtasPerSm)
+    bispec_accum_kernel(const __grid_constant__ CUtensorMap tmW, const __grid_constant__ CUtensorMap tmV,
+                        const __grid_constant__ CUtensorMap tmA, const BispecArgs p)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    bispec_unit<DE, EXACT>(smem, &tmW, &tmV, &tmA, p, (int)blockIdx.x);
 }
 
 // ---------------------------------------------------------------- host side
@@ -522,19 +541,12 @@ static bool make_map(CUtensorMap* m, const float2* S, int nframes, const Geometr
         == CUDA_SUCCESS;
 }
 
-template <int DE, bool EXACT>
-static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStream_t st)
+// The launch arguments of one batch: packed layout, tile list and the split
+// of the last partial wave's tiles by frames.
+template <int DE>
+static BispecArgs fill_args(const BispecLaunch& L, const Geometry& g)
 {
     using Cf = BCfg<DE>;
-    CUtensorMap mW, mV, mA;
-    if (!make_map(&mW, L.S, L.nframes, g, Cf::BW, Cf::RPC, Cf::FPS)
-        || !make_map(&mV, L.S, L.nframes, g, Cf::BV, Cf::RPC, Cf::FPS)
-        || !make_map(&mA, L.S, L.nframes, g, Cf::JT, 1, Cf::FPS))
-        return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(bispec_accum_kernel<DE, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         Cf::SMEM);
-    if (e != cudaSuccess)
-        return e;
     BispecArgs a;
     a.B = L.B;
     a.C = L.C;
@@ -569,8 +581,146 @@ static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStrea
     a.nsplit = P > 1 ? rem * P : 0;
     a.scratch = L.scratch;
     a.tile_cnt = L.tile_cnt;
+    return a;
+}
+
+template <int DE>
+static bool make_maps(CUtensorMap* m, const BispecLaunch& L, const Geometry& g)
+{
+    using Cf = BCfg<DE>;
+    return make_map(&m[0], L.S, L.nframes, g, Cf::BW, Cf::RPC, Cf::FPS)
+           && make_map(&m[1], L.S, L.nframes, g, Cf::BV, Cf::RPC, Cf::FPS)
+           && make_map(&m[2], L.S, L.nframes, g, Cf::JT, 1, Cf::FPS);
+}
+
+template <int DE, bool EXACT>
+static cudaError_t launch_de(const BispecLaunch& L, const Geometry& g, cudaStream_t st)
+{
+    using Cf = BCfg<DE>;
+    CUtensorMap m[3];
+    if (!make_maps<DE>(m, L, g))
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(bispec_accum_kernel<DE, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         Cf::SMEM);
+    if (e != cudaSuccess)
+        return e;
+    const BispecArgs a = fill_args<DE>(L, g);
     const int grid = a.nfull + a.nsplit;
-    bispec_accum_kernel<DE, EXACT><<<grid, Cf::THREADS, Cf::SMEM, st>>>(mW, mV, mA, a); note_launches(1);
+    bispec_accum_kernel<DE, EXACT><<<grid, Cf::THREADS, Cf::SMEM, st>>>(m[0], m[1], m[2], a); note_launches(1);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------- many stacks, one launch
+// A persistent grid (one CTA per SM) takes units from a device work list of
+// (stack, unit) pairs -- every stack's tiles and split-tile parts, exactly the
+// units its own launch would run, longest first -- so the bispectrum work of
+// stacks of any sizes and depths runs as one launch.  Each unit is the
+// single-stack kernel's unit (same tile decomposition, same split parts
+// merged in part order), so every stack's result is bit-identical to its own
+// launch.  Per stack the record below holds its three tensor maps over its
+// spectra and its launch arguments; records, work list and counter live in
+// device memory, so the launch itself never changes.
+struct MultiStackRec {
+    CUtensorMap m[3];
+    BispecArgs a;
+    int de;    // kernel depth class (a multiple of 8)
+    int exact; // the stack's depth is de itself
+};
+
+template <int DE> struct MaxSmem {
+    static constexpr int v = BCfg<DE>::SMEM > MaxSmem<DE - 8>::v ? BCfg<DE>::SMEM : MaxSmem<DE - 8>::v;
+};
+template <> struct MaxSmem<0> {
+    static constexpr int v = 0;
+};
+constexpr int kMultiSmem = MaxSmem<64>::v;
+
+// One unit as a separate function per depth class, so that each keeps the
+// register allocation of its own kernel inside the dispatching loop.
+template <int DE, bool EXACT>
+__device__ __noinline__ bool bispec_unit_call(unsigned char* smem, const MultiStackRec* r, int unit)
+{
+    return bispec_unit<DE, EXACT>(smem, &r->m[0], &r->m[1], &r->m[2], r->a, unit);
+}
+
+// ctrl[0]: work items; ctrl[1]: next item (zero at launch)
+__global__ void __launch_bounds__(512, 1) bispec_multi_kernel(const MultiStackRec* __restrict__ recs,
+                                                              const int2* __restrict__ items, int* ctrl)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int s_item;
+    const int nitems = *reinterpret_cast<volatile int*>(ctrl);
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        __syncthreads(); // every thread has read s_item
+        if (threadIdx.x == 0)
+            s_item = atomicAdd(&ctrl[1], 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= nitems)
+            break;
+        const int2 w = items[it];
+        const MultiStackRec* r = recs + w.x;
+        if (lane == 0) // the ring's issuers: lane 0 of any warp
+            for (int k = 0; k < 3; ++k)
+                asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(&r->m[k]) : "memory");
+        bool ok = true;
+        switch (r->de * 2 + r->exact) {
+#define SMIP_MULTI_CASE(DE)                                                                                       \
+    case 2 * DE + 1: ok = bispec_unit_call<DE, true>(smem, r, w.y); break;                                        \
+    case 2 * DE: ok = bispec_unit_call<DE, false>(smem, r, w.y); break;
+            SMIP_MULTI_CASE(8) SMIP_MULTI_CASE(16) SMIP_MULTI_CASE(24) SMIP_MULTI_CASE(32)
+            SMIP_MULTI_CASE(40) SMIP_MULTI_CASE(48) SMIP_MULTI_CASE(56) SMIP_MULTI_CASE(64)
+#undef SMIP_MULTI_CASE
+        default: break;
+        }
+        if (!__syncthreads_and(ok)) // a wait expired (recorded in the stack's error word): stop
+            break;
+    }
+}
+
+size_t bispec_multi_rec_bytes() { return sizeof(MultiStackRec); }
+
+int bispec_multi_fill(void* rec, const BispecLaunch& L, const Geometry& g, std::vector<int>* unit_frames)
+{
+    MultiStackRec r; // 64-byte aligned here, as the tensor-map encoder requires; copied out at the end
+    std::memset(&r, 0, sizeof r);
+    const int de = (g.De + 7) / 8 * 8;
+    r.de = de;
+    r.exact = g.De % 8 == 0;
+    bool ok = false;
+    switch (de) {
+#define SMIP_MULTI_FILL(DE)                                                                                       \
+    case DE: ok = make_maps<DE>(r.m, L, g); r.a = fill_args<DE>(L, g); break;
+        SMIP_MULTI_FILL(8) SMIP_MULTI_FILL(16) SMIP_MULTI_FILL(24) SMIP_MULTI_FILL(32)
+        SMIP_MULTI_FILL(40) SMIP_MULTI_FILL(48) SMIP_MULTI_FILL(56) SMIP_MULTI_FILL(64)
+#undef SMIP_MULTI_FILL
+    default: return -1;
+    }
+    if (!ok)
+        return -1;
+    // frames per unit: whole tiles take the batch, split units their part
+    const int units = r.a.nfull + r.a.nsplit;
+    unit_frames->resize(units);
+    for (int u = 0; u < units; ++u) {
+        if (u < r.a.nfull) {
+            (*unit_frames)[u] = L.nframes;
+        } else {
+            const int part = (u - r.a.nfull) % r.a.P;
+            (*unit_frames)[u] = (int)((long long)(part + 1) * L.nframes / r.a.P - (long long)part * L.nframes / r.a.P);
+        }
+    }
+    std::memcpy(rec, &r, sizeof r);
+    return units;
+}
+
+cudaError_t launch_bispec_multi(const void* recs, const int2* items, int* ctrl, int num_sms, cudaStream_t st)
+{
+    cudaError_t e = cudaFuncSetAttribute(bispec_multi_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMultiSmem);
+    if (e != cudaSuccess)
+        return e;
+    bispec_multi_kernel<<<num_sms, 512, kMultiSmem, st>>>(static_cast<const MultiStackRec*>(recs), items, ctrl);
+    note_launches(1);
     return cudaGetLastError();
 }
 

@@ -71,18 +71,30 @@ struct DeviceCtx {
     double2* tw64 = nullptr;
     dfc* twdf = nullptr;     // the same table as float-float (hi, lo)
     int num_sms = 0;
-    // smip_batch_launch: the streams the graphs launch on (round robin, so
-    // that consecutive calls' graphs overlap), their done events, the fork
-    // event of the capture, and executable graphs by topology (updated in
-    // place for a new call of the same topology)
-    static constexpr int kGraphStreams = 8;
+    // smip_batch_launch: the bispectrum work of many stacks as one persistent
+    // launch.  Two slots alternate; each holds page-locked host copies of the
+    // stack records, the work list and its control words, their device
+    // copies, and a CUDA graph captured once for the slot's buffers: the
+    // three host-to-device copies, then the persistent kernel.  A call fills
+    // the host side and launches the graph; the graph is captured again only
+    // when a slot's buffers grow.
+    struct MultiSlot {
+        unsigned char* h_recs = nullptr;
+        int2* h_items = nullptr;
+        int* h_ctrl = nullptr;
+        unsigned char* d_recs = nullptr;
+        int2* d_items = nullptr;
+        int* d_ctrl = nullptr;
+        size_t rec_cap = 0, item_cap = 0;
+        cudaGraphExec_t exec = nullptr;
+        cudaEvent_t ev_used = nullptr; // the slot's last launch has read its host buffers
+        bool used = false;
+    };
     std::shared_ptr<std::mutex> gmu = std::make_shared<std::mutex>();
-    cudaStream_t gst[kGraphStreams] = {};
-    cudaEvent_t ev_done[kGraphStreams] = {};
-    int gnext = 0;
-    cudaEvent_t ev_fork = nullptr;
-    std::shared_ptr<std::map<std::vector<int>, cudaGraphExec_t>> gexec =
-        std::make_shared<std::map<std::vector<int>, cudaGraphExec_t>>();
+    std::shared_ptr<MultiSlot> mslot = std::shared_ptr<MultiSlot>(new MultiSlot[2], std::default_delete<MultiSlot[]>());
+    int mnext = 0;
+    cudaStream_t mst = nullptr;     // the batch stream
+    cudaEvent_t ev_mdone = nullptr; // the last batch launch has finished
 };
 
 std::mutex g_ctx_mu;
@@ -482,9 +494,8 @@ struct smip_stack {
     // phase recovery and the final image: a high-priority stream
     cudaStream_t rst = nullptr;
     cudaEvent_t ev_reco = nullptr;
-    // smip_batch_launch: this stack's branch of the graph is captured on bst
-    cudaStream_t bst = nullptr;
-    cudaEvent_t ev_join = nullptr, ev_dep = nullptr;
+    // smip_batch_launch: the stack's per-frame kernels of the batch are done
+    cudaEvent_t ev_dep = nullptr;
 
     ~smip_stack()
     {
@@ -496,9 +507,6 @@ struct smip_stack {
             cudaStreamDestroy(rst);
         }
         if (ev_reco) cudaEventDestroy(ev_reco);
-        if (bst)
-            cudaStreamDestroy(bst);
-        if (ev_join) cudaEventDestroy(ev_join);
         if (ev_dep) cudaEventDestroy(ev_dep);
         dfree(B); dfree(C); dfree(Bn); dfree(P); dfree(Ppart);
         if (sum) cudaFree(sum);
@@ -632,7 +640,7 @@ struct smip_stack {
     // only).  wait_copies: order it after the batch's frame copies on cst
     // (a graph launch orders them outside the graph instead).  timed: CUDA
     // events around the bispectrum kernel.
-    int issue_batch(cudaStream_t q, bool wait_copies, bool timed)
+    int issue_batch(cudaStream_t q, bool wait_copies, bool timed, bool with_bispec = true)
     {
         const int n = pending;
         const long first_index = nframes - n;
@@ -685,15 +693,9 @@ struct smip_stack {
                                         g, shifts + 2 * first_index, q));
             CUDA_TRY(launch_saa_add(dtype, sum, staging, (long long)fe, n, first ? 1 : 0, shifts + 2 * first_index, g, q));
         }
-        BispecLaunch L;
-        L.S = S;
-        L.nframes = n;
-        L.B = B;
-        L.C = C;
-        L.err = err;
-        L.num_sms = ctx->num_sms;
-        L.scratch = kscratch;
-        L.tile_cnt = ktile_cnt;
+        if (!with_bispec)
+            return SMIP_OK;
+        const BispecLaunch L = bispec_launch(n);
         if (timed) {
             if (ev_used == ev_pool.size()) {
                 cudaEvent_t a, b;
@@ -711,6 +713,21 @@ struct smip_stack {
             ++ev_used;
         }
         return SMIP_OK;
+    }
+
+    // The bispectrum launch of a batch of n frames (spectra in S).
+    BispecLaunch bispec_launch(int n) const
+    {
+        BispecLaunch L;
+        L.S = S;
+        L.nframes = n;
+        L.B = B;
+        L.C = C;
+        L.err = err;
+        L.num_sms = ctx->num_sms;
+        L.scratch = kscratch;
+        L.tile_cnt = ktile_cnt;
+        return L;
     }
 
     // Host bookkeeping once the batch's work is issued and ev_free[cur] is
@@ -1007,11 +1024,47 @@ extern "C" int smip_stack_sync(smip_stack_t s)
     return check_dev_err(s->err, s->st);
 }
 
-// One CUDA graph for the pending batches of several stacks: each stack's
-// kernels form one branch, captured on the stack's own capture stream
-// between a fork and a join on one of the device's graph streams, so the
-// branches run concurrently.  Executable graphs are kept by topology and
-// updated in place for a later call of the same topology.
+// The pending batches of several stacks: each stack's per-frame kernels on
+// its own stream (concurrently), then the bispectrum work of all of them as
+// one persistent launch over a work list of every stack's units, longest
+// first (launch_bispec_multi), run by a CUDA graph captured once per slot
+// buffer set (the records and the work list travel in device memory).  Each
+// unit is what the stack's own launch would run, so results are identical to
+// smip_stack_flush on each stack.
+static int multi_slot_reserve(DeviceCtx::MultiSlot& m, size_t nrec, size_t nitem)
+{
+    if (nrec <= m.rec_cap && nitem <= m.item_cap)
+        return SMIP_OK;
+    if (m.used)
+        CUDA_TRY(cudaEventSynchronize(m.ev_used));
+    if (m.exec) {
+        cudaGraphExecDestroy(m.exec);
+        m.exec = nullptr;
+    }
+    const size_t rb = bispec_multi_rec_bytes();
+    if (nrec > m.rec_cap) {
+        if (m.h_recs) cudaFreeHost(m.h_recs);
+        if (m.d_recs) cudaFree(m.d_recs);
+        m.h_recs = m.d_recs = nullptr;
+        m.rec_cap = std::max<size_t>(nrec, 2 * m.rec_cap);
+        CUDA_TRY(cudaMallocHost(&m.h_recs, rb * m.rec_cap));
+        CUDA_TRY(cudaMalloc(&m.d_recs, rb * m.rec_cap));
+    }
+    if (nitem > m.item_cap) {
+        if (m.h_items) cudaFreeHost(m.h_items);
+        if (m.d_items) cudaFree(m.d_items);
+        m.h_items = m.d_items = nullptr;
+        m.item_cap = std::max<size_t>(nitem, 2 * m.item_cap);
+        CUDA_TRY(cudaMallocHost(&m.h_items, sizeof(int2) * m.item_cap));
+        CUDA_TRY(cudaMalloc(&m.d_items, sizeof(int2) * m.item_cap));
+    }
+    if (!m.h_ctrl) {
+        CUDA_TRY(cudaMallocHost(&m.h_ctrl, 2 * sizeof(int)));
+        CUDA_TRY(cudaMalloc(&m.d_ctrl, 2 * sizeof(int)));
+    }
+    return SMIP_OK;
+}
+
 extern "C" int smip_batch_launch(smip_stack_t* stacks, long count)
 {
     if (count < 0 || (count > 0 && !stacks))
@@ -1033,96 +1086,90 @@ extern "C" int smip_batch_launch(smip_stack_t* stacks, long count)
     DeviceCtx* ctx = L[0]->ctx;
     std::lock_guard<std::mutex> lk(*ctx->gmu);
     CUDA_TRY(cudaSetDevice(L[0]->device));
-    if (!ctx->ev_fork) {
-        CUDA_TRY(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
-        for (int k = 0; k < DeviceCtx::kGraphStreams; ++k) {
-            CUDA_TRY(cudaStreamCreateWithFlags(&ctx->gst[k], cudaStreamNonBlocking));
-            CUDA_TRY(cudaEventCreateWithFlags(&ctx->ev_done[k], cudaEventDisableTiming));
-        }
+    if (!ctx->mst) {
+        CUDA_TRY(cudaStreamCreateWithFlags(&ctx->mst, cudaStreamNonBlocking));
+        CUDA_TRY(cudaEventCreateWithFlags(&ctx->ev_mdone, cudaEventDisableTiming));
+        for (int k = 0; k < 2; ++k)
+            CUDA_TRY(cudaEventCreateWithFlags(&ctx->mslot.get()[k].ev_used, cudaEventDisableTiming));
     }
-    const int gk = ctx->gnext;
-    ctx->gnext = (gk + 1) % DeviceCtx::kGraphStreams;
-    cudaStream_t G = ctx->gst[gk];
-    // the graph's topology: per branch, frames or spectra and whether it
-    // holds the stack's first batch (reference frame work); and the graph
-    // stream, since launches of one executable graph run one after another
-    std::vector<int> topo { gk };
-    for (smip_stack* s : L)
-        topo.push_back(s->mode == 2 ? 2 : (s->has_ref ? 1 : 3));
-    for (smip_stack* s : L) {
+    // 1. every stack's per-frame kernels on its own stream
+    std::vector<int> npend(L.size());
+    for (size_t k = 0; k < L.size(); ++k) {
+        smip_stack* s = L[k];
+        npend[k] = s->pending;
         int rc = s->prepare_batch();
+        if (!rc)
+            rc = s->issue_batch(s->st, true, false, false);
         if (rc)
             return rc;
-        if (!s->bst) {
-            CUDA_TRY(cudaStreamCreateWithFlags(&s->bst, cudaStreamNonBlocking));
-            CUDA_TRY(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
+        if (s->mode != 2)
+            CUDA_TRY(cudaEventRecord(s->ev_free[s->cur], s->st)); // the frames' last reader
+        if (!s->ev_dep)
             CUDA_TRY(cudaEventCreateWithFlags(&s->ev_dep, cudaEventDisableTiming));
-        }
-        // the graph runs after the stack's earlier work and its batch's frame copies
         CUDA_TRY(cudaEventRecord(s->ev_dep, s->st));
-        CUDA_TRY(cudaStreamWaitEvent(G, s->ev_dep, 0));
-        if (s->mode != 2) {
-            CUDA_TRY(cudaEventRecord(s->ev_copied[s->cur], s->cst));
-            CUDA_TRY(cudaStreamWaitEvent(G, s->ev_copied[s->cur], 0));
-        }
     }
-    CUDA_TRY(cudaStreamBeginCapture(G, cudaStreamCaptureModeRelaxed));
-    int rc = SMIP_OK;
-    cudaError_t ce = cudaEventRecord(ctx->ev_fork, G);
-    for (size_t i = 0; i < L.size() && ce == cudaSuccess && rc == SMIP_OK; ++i) {
-        smip_stack* s = L[i];
-        ce = cudaStreamWaitEvent(s->bst, ctx->ev_fork, 0);
+    // 2. records and the work list, in the next slot's host buffers
+    DeviceCtx::MultiSlot& m = ctx->mslot.get()[ctx->mnext];
+    ctx->mnext ^= 1;
+    if (m.used)
+        CUDA_TRY(cudaEventSynchronize(m.ev_used)); // its previous launch has copied the host buffers
+    const size_t rb = bispec_multi_rec_bytes();
+    std::vector<std::vector<int>> uf(L.size());
+    std::vector<unsigned char> recs(rb * L.size());
+    size_t nitems = 0;
+    for (size_t k = 0; k < L.size(); ++k) {
+        const int units = bispec_multi_fill(recs.data() + rb * k, L[k]->bispec_launch(npend[k]), L[k]->g, &uf[k]);
+        if (units < 0)
+            return fail(SMIP_E_CUDA, "tensor map encoding failed");
+        nitems += (size_t)units;
+    }
+    int rc = multi_slot_reserve(m, L.size(), nitems);
+    if (rc)
+        return rc;
+    std::memcpy(m.h_recs, recs.data(), recs.size());
+    {   // longest units first (frames per unit), ties in stack and unit order
+        std::vector<std::pair<int, int2>> it;
+        it.reserve(nitems);
+        for (size_t k = 0; k < L.size(); ++k)
+            for (size_t u = 0; u < uf[k].size(); ++u)
+                it.push_back({ uf[k][u], make_int2((int)k, (int)u) });
+        std::stable_sort(it.begin(), it.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+        for (size_t q = 0; q < nitems; ++q)
+            m.h_items[q] = it[q].second;
+    }
+    m.h_ctrl[0] = (int)nitems;
+    m.h_ctrl[1] = 0;
+    // 3. the slot's graph on the batch stream, after every stack's per-frame kernels
+    for (smip_stack* s : L)
+        CUDA_TRY(cudaStreamWaitEvent(ctx->mst, s->ev_dep, 0));
+    if (!m.exec) {
+        cudaGraph_t graph = nullptr;
+        CUDA_TRY(cudaStreamBeginCapture(ctx->mst, cudaStreamCaptureModeRelaxed));
+        cudaError_t ce = cudaMemcpyAsync(m.d_recs, m.h_recs, rb * m.rec_cap, cudaMemcpyHostToDevice, ctx->mst);
         if (ce == cudaSuccess)
-            rc = s->issue_batch(s->bst, false, false);
-        if (ce == cudaSuccess && rc == SMIP_OK)
-            ce = cudaEventRecord(s->ev_join, s->bst);
-        if (ce == cudaSuccess && rc == SMIP_OK)
-            ce = cudaStreamWaitEvent(G, s->ev_join, 0);
-    }
-    cudaGraph_t graph = nullptr;
-    const cudaError_t ee = cudaStreamEndCapture(G, &graph);
-    if (rc != SMIP_OK || ce != cudaSuccess || ee != cudaSuccess) {
+            ce = cudaMemcpyAsync(m.d_items, m.h_items, sizeof(int2) * m.item_cap, cudaMemcpyHostToDevice, ctx->mst);
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(m.d_ctrl, m.h_ctrl, 2 * sizeof(int), cudaMemcpyHostToDevice, ctx->mst);
+        if (ce == cudaSuccess)
+            ce = launch_bispec_multi(m.d_recs, m.d_items, m.d_ctrl, ctx->num_sms, ctx->mst);
+        const cudaError_t ee = cudaStreamEndCapture(ctx->mst, &graph);
+        if (ce == cudaSuccess && ee == cudaSuccess)
+            ce = cudaGraphInstantiate(&m.exec, graph, 0);
         if (graph)
             cudaGraphDestroy(graph);
-        cudaGetLastError();
-        if (rc != SMIP_OK)
-            return rc;
-        return fail(SMIP_E_CUDA, cudaGetErrorString(ce != cudaSuccess ? ce : ee));
-    }
-    auto& cache = *ctx->gexec;
-    cudaGraphExec_t exec = nullptr;
-    auto it = cache.find(topo);
-    if (it != cache.end()) {
-        cudaGraphExecUpdateResultInfo info;
-        if (cudaGraphExecUpdate(it->second, graph, &info) == cudaSuccess) {
-            exec = it->second;
-        } else {
+        if (ce != cudaSuccess || ee != cudaSuccess) {
             cudaGetLastError();
-            cudaGraphExecDestroy(it->second); // freed once a launch still in flight completes
-            cache.erase(it);
+            m.exec = nullptr;
+            return fail(SMIP_E_CUDA, cudaGetErrorString(ce != cudaSuccess ? ce : ee));
         }
     }
-    if (!exec) {
-        if (cache.size() >= 64) { // bounded: drop them all
-            for (auto& e : cache)
-                cudaGraphExecDestroy(e.second);
-            cache.clear();
-        }
-        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-        if (ie != cudaSuccess) {
-            cudaGraphDestroy(graph);
-            return fail(SMIP_E_CUDA, cudaGetErrorString(ie));
-        }
-        cache[topo] = exec;
-    }
-    cudaGraphDestroy(graph);
-    CUDA_TRY(cudaGraphLaunch(exec, G));
-    CUDA_TRY(cudaEventRecord(ctx->ev_done[gk], G));
+    CUDA_TRY(cudaGraphLaunch(m.exec, ctx->mst));
+    CUDA_TRY(cudaEventRecord(m.ev_used, ctx->mst));
+    m.used = true;
+    CUDA_TRY(cudaEventRecord(ctx->ev_mdone, ctx->mst));
     for (smip_stack* s : L) {
-        // later work on the stack's stream, and the refill of its frame buffer, follow the graph
-        CUDA_TRY(cudaStreamWaitEvent(s->st, ctx->ev_done[gk], 0));
-        if (s->mode != 2)
-            CUDA_TRY(cudaEventRecord(s->ev_free[s->cur], G));
+        // the stack's later work (its next batch overwrites the spectra) follows the launch
+        CUDA_TRY(cudaStreamWaitEvent(s->st, ctx->ev_mdone, 0));
         s->commit_batch();
     }
     return SMIP_OK;

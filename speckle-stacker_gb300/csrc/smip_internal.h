@@ -126,6 +126,17 @@ struct BispecLaunch {
 };
 cudaError_t launch_bispec_accumulate(const BispecLaunch& L, const Geometry& g, cudaStream_t st);
 size_t bispec_scratch_bytes(int num_sms);
+
+// Many stacks' batches in one persistent launch (k_bispec.cu).  A record per
+// stack (bispec_multi_rec_bytes() bytes, 64-byte aligned) holds its tensor
+// maps and launch arguments; bispec_multi_fill writes it for the batch L and
+// returns the stack's unit count (tiles and split-tile parts, as its own
+// launch would run them) with each unit's frames, or -1.  The launch takes
+// units from items[0 .. ctrl[0]) = (record, unit), counting ctrl[1] up from
+// zero; records, items and ctrl are device memory.
+size_t bispec_multi_rec_bytes();
+int bispec_multi_fill(void* rec, const BispecLaunch& L, const Geometry& g, std::vector<int>* unit_frames);
+cudaError_t launch_bispec_multi(const void* recs, const int2* items, int* ctrl, int num_sms, cudaStream_t st);
 // diagnostic: two bounded waits that can never be satisfied (see smip_diag_bounded_wait)
 cudaError_t launch_bounded_wait_probe(int* err, const int* never, double timeout_s, cudaStream_t st);
 size_t bispec_tile_counters(int num_sms);

@@ -161,9 +161,10 @@ def version():
 
 
 def batch_launch(stacks) -> None:
-    """Runs the pending frame batches of ``stacks`` as one CUDA graph launch
-    (one concurrent branch per stack); stacks without pending frames are
-    skipped.  Later calls on each stack are ordered after the graph."""
+    """Runs the pending frame batches of ``stacks``: each stack's per-frame
+    kernels on its own stream, then the bispectrum work of all of them as one
+    persistent launch (a CUDA graph captured once); stacks without pending
+    frames are skipped.  Later calls on each stack are ordered after it."""
     stacks = list(stacks)
     arr = (C.c_void_p * max(1, len(stacks)))(*[st._h.value for st in stacks])
     _check(_L().smip_batch_launch(arr, len(stacks)))

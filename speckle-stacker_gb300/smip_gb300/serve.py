@@ -136,7 +136,8 @@ class Engine:
     workers: threads that run phase recovery + the final image.
     stack_factory: (ncols, nrows, bdepth) -> stack; defaults to smip_gb300.Stack.
     graph: the last batches of the jobs whose frames are all in after a round
-        run as one CUDA graph launch (smip_gb300.batch_launch) before their
+        run together (smip_gb300.batch_launch: their bispectrum work as one
+        persistent launch from a captured CUDA graph) before their
         reconstructions start, instead of one flush per job.
     stall_timeout: seconds a streaming job may go without new frames from its
         producer before it fails (None: wait for ever).

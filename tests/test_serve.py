@@ -106,13 +106,15 @@ def test_engine_pool_reuses_stacks():
 
 @pytest.mark.gpu
 def test_results_same_alone_and_in_mix(smip):
-    """Jobs of mixed sizes (64^2 binary u8, 128^2 extended u16, uneven counts)
-    served concurrently give exactly the results each gives alone."""
-    jobs = serve.make_jobs(6, sizes=(64, 128), counts=(30, 300), bank_frames=64, seed=11)
+    """Jobs of mixed sizes (64^2, 128^2 and 256^2, binary u8 and extended u16,
+    uneven counts) served concurrently give exactly the results each gives
+    alone."""
+    jobs = serve.make_jobs(8, sizes=(64, 128, 256), counts=(30, 300), bank_frames=64, seed=11)
+    assert {j.shape[0] for j in jobs} == {64, 128, 256}
     alone, _ = serve.run_plain(jobs, realtime=False)
     by_id = {r.id: r for r in alone}
-    for graph in (False, True):  # last batches flushed per job, or one CUDA graph per round
-        eng = serve.Engine(max_active=6, workers=3, graph=graph)
+    for graph in (False, True):  # last batches flushed per job, or one persistent launch per round
+        eng = serve.Engine(max_active=8, workers=3, graph=graph)
         eng.prewarm({j.shape for j in jobs}, count=3)
         mixed, _ = eng.run(jobs, realtime=False)
         assert eng.peak_active >= 2
@@ -170,21 +172,23 @@ def test_autotune_on_device(smip, tmp_path, monkeypatch):
 
 @pytest.mark.gpu
 def test_batch_launch_matches_flush(smip):
-    """One CUDA graph over the pending batches of several stacks (uneven
-    shapes, depths and counts; some batches already launched on their own)
-    gives bit-identical results to flushing each stack, also when the graph
-    of the previous call is updated in place."""
+    """One persistent bispectrum launch over the pending batches of several
+    stacks (uneven shapes, depths and counts, an odd frame size, a depth that
+    is not a multiple of 8; some batches already launched on their own) gives
+    bit-identical results to flushing each stack, over repeated calls that
+    reuse the captured graphs."""
     rng = np.random.default_rng(5)
-    cfg = [(64, 16, 50), (128, 24, 130), (64, 16, 70), (256, 32, 40), (64, 16, 64)]
-    frames = [rng.integers(0, 4096, (nf, n, n)).astype(np.uint16) for n, d, nf in cfg]
+    cfg = [(64, 64, 16, 50), (128, 128, 24, 130), (64, 64, 16, 70), (256, 256, 32, 40), (64, 64, 16, 64),
+           (99, 75, 20, 45), (48, 48, 8, 30)]
+    frames = [rng.integers(0, 4096, (nf, h, w)).astype(np.uint16) for w, h, d, nf in cfg]
 
     def results(st):
         return st.shifts(), st.sum(), st.power(), st.bispectrum()
 
     def run(graph):
-        stacks = [smip.Stack(n, n, d, batch_frames=64) for n, d, _ in cfg]
+        stacks = [smip.Stack(w, h, d, batch_frames=64) for w, h, d, _ in cfg]
         out = []
-        for rnd in range(2):
+        for rnd in range(3):
             for st, fr in zip(stacks, frames):
                 st.reset()
                 st.push_frames(fr[rnd:])  # 64 frames run as a batch during the push
