@@ -266,8 +266,10 @@ def run_reference(args):
 
 BATCHED_DESC = ("64 independent stacks queued at once, each pushed whole: frame size from {64,128,256}, frames uniform in 50-1000, "
                 "binary u8 / extended u16 objects 50/50, depth 16/24/32 by size, reco radius 2 x depth")
-SERVED_DESC = ("Poisson arrivals at 20 jobs/s, 40 jobs, frame size from {64,128,256}, 100-2000 frames per job "
-               "delivered in 32-frame chunks, admission by bispectrum bytes under a 120 GB budget")
+SERVED_DESC = ("Poisson arrivals at 20 jobs/s for 60 s (1200 jobs), frame size from {64,128,256}, 100-2000 frames "
+               "per job delivered in 32-frame chunks, admission by bispectrum bytes under a 120 GB budget")
+SWEEP_RATES = (100.0, 200.0, 400.0)
+SWEEP_JOBS = 240
 
 
 def make_serving_jobs(procs):
@@ -277,48 +279,141 @@ def make_serving_jobs(procs):
 
     # a queued stack is complete: one push per stack (the served workload below streams 32-frame chunks)
     batched = serve.make_jobs(64, counts=(50, 1000), rate=None, seed=3000, bank_frames=256, procs=procs, chunk=1000)
-    served = serve.make_jobs(40, counts=(100, 2000), rate=20.0, seed=4000, bank_frames=256, procs=procs)
-    return batched, served
+    served = serve.make_jobs(1200, counts=(100, 2000), rate=20.0, seed=4000, bank_frames=256, procs=procs)
+    sweep = {r: serve.make_jobs(SWEEP_JOBS, counts=(100, 2000), rate=r, seed=5000 + int(r), bank_frames=256,
+                                procs=procs) for r in SWEEP_RATES}
+    return batched, served, sweep
 
 
 def serving_metrics(jobs):
     """Batched and served execution against the plain single-job path on the
     same jobs: frames/s, p50/p99 job latency, and whether every job's results
-    are identical in both."""
+    are identical in both.  batched: config 3, all 64 stacks at once (best of
+    two runs of each path; host thread scheduling varies run to run).
+    served: config 4, 60 s of Poisson arrivals at 20 jobs/s.  served_sweep:
+    the same job mix at higher arrival rates, up to and past saturation of
+    both paths."""
     from smip_gb300 import serve
 
-    batched, served = jobs
-    keep = serve.pin_banks(batched + served)
+    batched, served, sweep = jobs
+    keep = serve.pin_banks(batched + served + [j for jl in sweep.values() for j in jl])
     shapes = {j.shape for j in batched + served}
     out = {}
-    for key, jl, realtime, desc in (("batched", batched, False, BATCHED_DESC), ("served", served, True, SERVED_DESC)):
-        eng = serve.Engine(budget_bytes=120e9, max_active=64, workers=32)
-        eng.prewarm(shapes, count=24)
-        eng_g = serve.Engine(budget_bytes=120e9, max_active=64, workers=32, graph=True)
-        eng_g.prewarm(shapes, count=24)
-        serve.run_plain(jl[:3], realtime=False)  # warm the code paths
-        eng_g.run(jl[:8], realtime=False)
-        # best of two runs of each (host thread scheduling varies run to run)
-        runs_s = [eng.run(jl, realtime=realtime) for _ in range(2)]
-        runs_g = [eng_g.run(jl, realtime=realtime) for _ in range(2)]
-        runs_p = [serve.run_plain(jl, realtime=realtime) for _ in range(2)]
-        eng.reco_mode = "rings"  # the opt-in ring-parallel phase recovery, same engine
-        runs_r = [eng.run(jl, realtime=realtime) for _ in range(2)]
-        eng.reco_mode = "spiral"
-        res_s, span_s = min(runs_s, key=lambda x: x[1])
-        res_g, span_g = min(runs_g, key=lambda x: x[1])
-        res_p, span_p = min(runs_p, key=lambda x: x[1])
+    eng = serve.Engine(budget_bytes=120e9, max_active=64, workers=32)
+    eng.prewarm(shapes, count=24)
+    eng_m = serve.Engine(budget_bytes=120e9, max_active=64, workers=32, graph=True)
+    eng_m.prewarm(shapes, count=24)
+    serve.run_plain(batched[:3], realtime=False)  # warm the code paths
+    eng_m.run(batched[:8], realtime=False)
+    runs_s = [eng.run(batched, realtime=False) for _ in range(2)]
+    runs_m = [eng_m.run(batched, realtime=False) for _ in range(2)]
+    runs_p = [serve.run_plain(batched, realtime=False) for _ in range(2)]
+    eng.reco_mode = "rings"  # the opt-in ring-parallel phase recovery, same engine
+    runs_r = [eng.run(batched, realtime=False) for _ in range(2)]
+    eng.reco_mode = "spiral"
+    res_s, span_s = min(runs_s, key=lambda x: x[1])
+    res_m, span_m = min(runs_m, key=lambda x: x[1])
+    res_p, span_p = min(runs_p, key=lambda x: x[1])
+    s, p = serve.summarize(res_s, span_s), serve.summarize(res_p, span_p)
+    sm = serve.summarize(res_m, span_m)
+    out["batched"] = {"workload": BATCHED_DESC, "served": s, "plain": p,
+                      "frames_per_s_ratio": s["frames_per_s"] / p["frames_per_s"],
+                      "results_identical": serve.compare_results(res_s, res_p),
+                      "peak_jobs_in_flight": eng.peak_active,
+                      "served_multi": sm, "frames_per_s_ratio_multi": sm["frames_per_s"] / p["frames_per_s"],
+                      "results_identical_multi": serve.compare_results(res_m, res_p),
+                      "served_rings": serve.summarize(*min(runs_r, key=lambda x: x[1]))}
+    del eng_m
+    # 60 s of arrivals at 20 jobs/s, served and plain
+    eng.peak_active = 0
+    res_s, span_s = eng.run(served, realtime=True)
+    peak = eng.peak_active
+    res_p, span_p = serve.run_plain(served, realtime=True)
+    s, p = serve.summarize(res_s, span_s), serve.summarize(res_p, span_p)
+    out["served"] = {"workload": SERVED_DESC, "served": s, "plain": p,
+                     "frames_per_s_ratio": s["frames_per_s"] / p["frames_per_s"],
+                     "results_identical": serve.compare_results(res_s, res_p), "peak_jobs_in_flight": peak}
+    # arrival-rate sweep
+    pts = []
+    for rate in SWEEP_RATES:
+        jl = sweep[rate]
+        eng.peak_active = 0
+        res_s, span_s = eng.run(jl, realtime=True)
+        peak = eng.peak_active
+        res_p, span_p = serve.run_plain(jl, realtime=True)
         s, p = serve.summarize(res_s, span_s), serve.summarize(res_p, span_p)
-        sg = serve.summarize(res_g, span_g)
-        out[key] = {"workload": desc, "served": s, "plain": p,
+        offered = sum(len(j.frames) for j in jl) / max(j.arrival for j in jl)
+        pts.append({"rate_jobs_per_s": rate, "offered_frames_per_s": offered, "served": s, "plain": p,
                     "frames_per_s_ratio": s["frames_per_s"] / p["frames_per_s"],
-                    "results_identical": serve.compare_results(res_s, res_p),
-                    "peak_jobs_in_flight": eng.peak_active,
-                    "served_multi": sg, "frames_per_s_ratio_multi": sg["frames_per_s"] / p["frames_per_s"],
-                    "results_identical_multi": serve.compare_results(res_g, res_p),
-                    "served_rings": serve.summarize(*min(runs_r, key=lambda x: x[1]))}
-        del eng, eng_g
-    del keep
+                    "peak_jobs_in_flight": peak, "results_identical": serve.compare_results(res_s, res_p)})
+    out["served_sweep"] = {"workload": f"{SWEEP_JOBS} jobs per rate, the served job mix, Poisson arrivals; the "
+                                       "reference's spiral phase recovery", "points": pts}
+    del eng, keep
+    return out
+
+
+LARGE_DESC = ("extended512: 10000 x 512x512 u16 (200 blobs + disk, D/r0=25), bispectrum depth 48, reco radius 200, "
+              "shift-and-add across all frames; the 10000 frames cycle through 512 distinct seeded frames")
+
+
+def large_stack_metrics(G, torch, dev, bank, steps=2):
+    """The largest configuration at full length: 10000 frames of 512x512 u16
+    (a cycled bank of distinct frames; kernel time does not depend on
+    content), depth 48, radius 200.  Frames resident in HBM (5.2 GB) and end
+    to end from page-locked host memory, plus the reconstruction latency."""
+    from smip_gb300 import synthetic as S
+
+    spec = S.config_spec("extended512")
+    nf = spec.nframes
+    reps = (nf + len(bank) - 1) // len(bank)
+    b16 = torch.from_numpy(bank.view(np.int16))
+    frames_dev = b16.to(dev).repeat(reps, 1, 1)[:nf].contiguous()
+    pinned = torch.empty((nf,) + tuple(bank.shape[1:]), dtype=torch.int16, pin_memory=True)
+    for k in range(reps):
+        lo, hi = k * len(bank), min(nf, (k + 1) * len(bank))
+        pinned[lo:hi].copy_(b16[:hi - lo])
+    pinned_np = pinned.numpy().view(np.uint16)
+    stream = torch.cuda.Stream(device=dev)
+    out = {"workload": LARGE_DESC}
+    with G.Stack(spec.n, spec.n, spec.bdepth, device=dev.index, stream=stream.cuda_stream) as st:
+        def step():
+            st.reset()
+            st.push_frames(frames_dev.view(torch.uint16))
+            st.flush()
+
+        step()
+        st.kernel_time()
+        st.set_timing(True)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        el = e0.elapsed_time(e1) * 1e-3
+        k2_ms, k2_n, k2_frames = st.kernel_time()
+        st.set_timing(False)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            st.reset()
+            st.push_frames(pinned_np)
+            sh = st.shifts()
+        e2e_el = time.perf_counter() - t0
+        rec = []
+        for _ in range(3):
+            t = time.perf_counter()
+            st.finish(float(spec.reco_radius))
+            rec.append((time.perf_counter() - t) * 1e3)
+    T = triples(spec.n, spec.bdepth)
+    out.update({"frames_per_step": nf, "steps": steps, "value": nf * steps / el, "unit": "frames/s",
+                "ms_per_step": 1e3 * el / steps,
+                "e2e": {"value": nf * steps / e2e_el, "unit": "frames/s", "h2d_bytes_per_step": int(nf * bank[0].nbytes),
+                        "d2h_bytes_per_step": int(sh.nbytes)},
+                "bispec_kernel_frames_per_s": k2_frames / (k2_ms * 1e-3) if k2_ms > 0 else None,
+                "bispec_kernel_tflops": 14.0 * T * k2_frames / (k2_ms * 1e-3) / 1e12 if k2_ms > 0 else None,
+                "bispec_launches": k2_n, "recon_p50_ms": float(np.percentile(rec, 50))})
+    del frames_dev, pinned
     return out
 
 
@@ -341,6 +436,9 @@ def run_ours(args):
     serve_jobs = None
     if rank == 0 and world == 1 and not args.no_serve and args.workload == WORKLOAD:
         serve_jobs = make_serving_jobs(procs)
+    large_bank = None
+    if rank == 0 and world == 1 and not args.no_large and args.workload == WORKLOAD:
+        large_bank = gen_frames(S.config_spec("extended512"), 512, procs)
     t_gen = time.perf_counter() - t_gen
 
     torch.cuda.set_device(local)
@@ -493,6 +591,7 @@ def run_ours(args):
         # one whole default batch: 1024 frames at 256x256, 288 at 512x512
         cpu["check"] = accuracy_check(G, spec, frames[:1024 if n <= 256 else 288], local)
     serving = serving_metrics(serve_jobs) if serve_jobs else None
+    large = large_stack_metrics(G, torch, dev, large_bank) if large_bank is not None else None
     line = {
         "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
@@ -508,6 +607,10 @@ def run_ours(args):
         "bispec_kernel_frames_per_s": (k2_frames / (k2_ms * 1e-3)) if k2_ms > 0 else None,
         "frame_generation_s": t_gen,
     }
+    if large:
+        large["bispec_kernel_frac_of_fp32_peak"] = (large["bispec_kernel_tflops"] / peak
+                                                    if large["bispec_kernel_tflops"] else None)
+        line["extended512"] = large
     if serving:
         for k in ("batched", "served"):
             if k in serving and "served_rings" in serving[k]:
@@ -534,6 +637,7 @@ def main():
     ap.add_argument("--nframes", type=int, default=None, help="frames of the stack (default: the workload's own)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the batched and served measurements")
+    ap.add_argument("--no-large", action="store_true", help="skip the 10000 x 512x512 measurement")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

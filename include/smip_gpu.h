@@ -95,6 +95,16 @@ SMIP_GPU_API int smip_stack_destroy(smip_stack_t s);
 SMIP_GPU_API int smip_stack_push_frames(smip_stack_t s, const void* frames, int dtype, long count,
                                         long frame_stride_bytes, int on_device);
 
+/* Tuning of the stack's bispectrum kernel (no counterpart in the reference):
+ * variant 0 stages four frames per shared-memory ring stage, 1 two;
+ * min_part_frames is the fewest frames a split part of a last-wave tile gets
+ * (0 = 8; a batch's last partial wave of tiles is split by frames so that it
+ * fills the GPU).  Neither changes which triples are summed; the split
+ * changes the order of a tile's partial sums, so results stay within the
+ * parity tolerances and a stack with the same settings gives the same bits.
+ * smip_gb300.autotune picks both per shape. */
+SMIP_GPU_API int smip_stack_set_kernel_config(smip_stack_t s, int variant, int min_part_frames);
+
 /* Phase-recovery estimator for smip_stack_reconstruct / smip_stack_finish.
  * SMIP_RECO_SPIRAL (default): the reference's walk (phasereco.h:33-123), each
  * point from every pair whose phases exist when the spiral reaches it.

@@ -442,6 +442,8 @@ struct smip_stack {
     int Bf = 0;                   // frames per batch
     int fpc = 16;                 // frames per column-pass chunk
     int dtype = -1;               // frame dtype fixed by the first push
+    int kvariant = 0;             // bispectrum kernel staging (smip_stack_set_kernel_config)
+    int kmin_part = 0;            // frames per split-tile part at least (0: the kernel's 8)
     int mode = 0;                 // 0 unset, 1 frames, 2 spectra
     long nframes = 0;             // frames accumulated (incl. pending)
     int pending = 0;              // frames staged for the next batch
@@ -727,6 +729,8 @@ struct smip_stack {
         L.num_sms = ctx->num_sms;
         L.scratch = kscratch;
         L.tile_cnt = ktile_cnt;
+        L.variant = kvariant;
+        L.min_part = kmin_part;
         return L;
     }
 
@@ -912,6 +916,18 @@ extern "C" int smip_stack_push_frames(smip_stack_t s, const void* frames, int dt
                 return rc;
         }
     }
+    return SMIP_OK;
+}
+
+extern "C" int smip_stack_set_kernel_config(smip_stack_t s, int variant, int min_part_frames)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    if (variant < 0 || variant > 1 || min_part_frames < 0)
+        return fail(SMIP_E_INVALID_ARGUMENT, "kernel variant must be 0 or 1 and min_part_frames >= 0");
+    s->kvariant = variant;
+    s->kmin_part = min_part_frames;
     return SMIP_OK;
 }
 

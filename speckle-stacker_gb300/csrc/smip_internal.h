@@ -123,8 +123,11 @@ struct BispecLaunch {
     int num_sms;
     float2* scratch;     // bispec_scratch_bytes(num_sms): partial sums of split tiles
     int* tile_cnt;       // bispec_tile_counters(num_sms) ints, zeroed once: parts finished per split tile
+    int variant = 0;     // kernel staging: 0 four frames per ring stage, 1 two
+    int min_part = 0;    // frames per split-tile part at least (0: 8)
 };
 cudaError_t launch_bispec_accumulate(const BispecLaunch& L, const Geometry& g, cudaStream_t st);
+cudaError_t launch_bispec_accumulate_fps2(const BispecLaunch& L, const Geometry& g, cudaStream_t st);
 size_t bispec_scratch_bytes(int num_sms);
 
 // Many stacks' batches in one persistent launch (k_bispec.cu).  A record per

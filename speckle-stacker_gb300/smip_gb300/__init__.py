@@ -103,6 +103,7 @@ def _load():
         "smip_stack_reconstruct": ([vp, C.c_double, dp, ubp, dp], C.c_int),
         "smip_stack_finish": ([vp, C.c_double, dp, dp, ubp, dp], C.c_int),
         "smip_stack_merge": ([vp, vp], C.c_int),
+        "smip_stack_set_kernel_config": ([vp, C.c_int, C.c_int], C.c_int),
         "smip_batch_launch": ([C.POINTER(vp), C.c_long], C.c_int),
         "smip_diag_bounded_wait": ([C.c_int, C.c_double], C.c_int),
         "smip_stack_set_bispectrum": ([vp, fp, C.c_long], C.c_int),
@@ -196,15 +197,19 @@ class Stack:
         """batch_frames: frames per accumulation batch; 0 = library default,
         "auto" = the autotuner's cached best for this device and shape (tuned
         on first use, smip_gb300.autotune); dtype only informs "auto"."""
+        tuned = None
         if batch_frames == "auto":
             from smip_gb300 import autotune
 
-            batch_frames = autotune.best_batch(ncols, nrows, bdepth, dtype, device)
+            tuned = autotune.best_config(ncols, nrows, bdepth, dtype, device)
+            batch_frames = tuned["batch_frames"]
         h = C.c_void_p()
         _check(_L().smip_stack_create(C.byref(h), device, ncols, nrows, bdepth,
                                       C.c_void_p(stream) if stream else None, batch_frames))
         self._h = h
         self.ncols, self.nrows, self.bdepth, self.device = ncols, nrows, bdepth, device
+        if tuned is not None:
+            self.set_kernel_config(tuned["variant"], tuned["min_part"])
 
     def close(self):
         if getattr(self, "_h", None):
@@ -254,6 +259,12 @@ class Stack:
         if a.ndim == 2:
             a = a[None]
         _check(_L().smip_stack_accumulate_fft(self._h, a.ctypes.data, a.shape[0], 0))
+
+    def set_kernel_config(self, variant: int = 0, min_part: int = 0):
+        """Bispectrum kernel tuning: variant 0 (four frames per ring stage) or
+        1 (two); min_part: fewest frames per split part of a last-wave tile
+        (0 = 8).  The autotuner picks both ("auto" batch_frames)."""
+        _check(_L().smip_stack_set_kernel_config(self._h, int(variant), int(min_part)))
 
     def set_reco_mode(self, mode="spiral"):
         """Phase-recovery estimator: "spiral" (default, the reference's walk)

@@ -143,12 +143,15 @@ class Engine:
         producer before it fails (None: wait for ever).
     reco_mode: "spiral" (the reference's phase recovery, default) or "rings"
         (the opt-in ring-parallel estimator, Stack.set_reco_mode).
+    chunks_per_round: a streaming job pushes up to this many of its delivered
+        chunks per round (whole chunks), so that the request loop's host
+        work per frame stays small when many jobs stream at once.
     """
 
     def __init__(self, device: int = 0, budget_bytes: float = 120e9, max_active: int = 64, workers: int = 32,
                  stack_factory: Optional[Callable] = None, graph: bool = False,
                  batch_launch: Optional[Callable] = None, stall_timeout: Optional[float] = None,
-                 reco_mode: str = "spiral"):
+                 reco_mode: str = "spiral", chunks_per_round: int = 8):
         if stack_factory is None:
             from smip_gb300 import Stack
 
@@ -164,6 +167,7 @@ class Engine:
         self.workers = int(workers)
         self.stall_timeout = stall_timeout
         self.reco_mode = reco_mode
+        self.chunks_per_round = max(1, int(chunks_per_round))
         self.pool: Dict[Tuple[int, int, int], list] = {}
         self.peak_bytes = 0.0
         self.peak_active = 0
@@ -255,7 +259,7 @@ class Engine:
                     active.append([job, self._acquire(job.shape), 0, now, need, now])
                 self.peak_bytes = max(self.peak_bytes, used)
                 self.peak_active = max(self.peak_active, len(active) + len(running))
-                # one chunk per streaming job, round robin
+                # the delivered chunks of every streaming job, round robin
                 pushed = False
                 ready = []
                 for entry in list(active):
@@ -264,7 +268,10 @@ class Engine:
                     if self._is_cancelled(job.id):
                         why = "cancelled"
                     else:
-                        k = min(job.chunk, job.available() - pos, len(job.frames) - pos)
+                        avail = min(job.available(), len(job.frames)) - pos
+                        k = min(job.chunk * self.chunks_per_round, avail)
+                        if k < avail:  # whole chunks only, unless it is the job's last piece
+                            k -= k % job.chunk
                         if k > 0:
                             try:
                                 for part in job.parts(pos, k):

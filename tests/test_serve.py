@@ -127,22 +127,25 @@ def test_results_same_alone_and_in_mix(smip):
 
 
 def test_autotune_cache_roundtrip(tmp_path, monkeypatch):
-    """best_batch tunes once per (device, shape, depth, dtype) and then reads
-    the cache; the measurement itself is replaced by a stand-in here."""
+    """best_config tunes the batch size, then the kernel's staging variant and
+    split, once per (device, shape, depth, dtype) and then reads the cache;
+    the measurement itself is replaced by a stand-in here."""
     from smip_gb300 import autotune
 
     monkeypatch.setattr(autotune, "CACHE", str(tmp_path / "at.json"))
     monkeypatch.setattr(autotune, "_device_name", lambda d: "dev")
     calls = []
 
-    def fake_measure(nc, nr, d, bf, frames, device=0, repeats=2):
-        calls.append(bf)
-        return 1000.0 - abs(bf - 256)  # best at 256
+    def fake_measure(nc, nr, d, bf, frames, device=0, repeats=2, kernel=(0, 0)):
+        calls.append((bf, kernel))
+        return 1000.0 - abs(bf - 256) + (5.0 if kernel == (1, 32) else 0.0)  # best at 256, variant 1, parts >= 32
 
     monkeypatch.setattr(autotune, "measure", fake_measure)
+    assert autotune.best_config(64, 64, 16, np.uint8) == {"batch_frames": 256, "variant": 1, "min_part": 32}
     assert autotune.best_batch(64, 64, 16, np.uint8) == 256
     n = len(calls)
-    assert n == len(autotune.CANDIDATES)
+    assert n == len(autotune.CANDIDATES) + len(autotune.KERNEL_CANDIDATES)
+    assert all(bf == 256 for bf, _ in calls[len(autotune.CANDIDATES):])  # kernel tunables at the best batch
     assert autotune.best_batch(64, 64, 16, np.uint8) == 256 and len(calls) == n  # cached
     assert autotune.best_batch(64, 64, 17, np.uint8) == 256 and len(calls) == n  # depth 17 acts as 16
     autotune.best_batch(64, 64, 16, np.uint16)
@@ -152,13 +155,14 @@ def test_autotune_cache_roundtrip(tmp_path, monkeypatch):
 @pytest.mark.gpu
 def test_autotune_on_device(smip, tmp_path, monkeypatch):
     """A real (small) tuning run picks one of the candidates and the stack it
-    configures gives the same bispectrum as the default batch size."""
+    configures gives the same bispectrum as the default batch size; the two
+    staging variants give the same bits."""
     from smip_gb300 import autotune
 
     monkeypatch.setattr(autotune, "CACHE", str(tmp_path / "at.json"))
     monkeypatch.setattr(autotune, "CANDIDATES", (16, 32, 64))
-    bf = autotune.best_batch(32, 32, 8, np.uint8)
-    assert bf in (16, 32, 64)
+    cfg = autotune.best_config(32, 32, 8, np.uint8)
+    assert cfg["batch_frames"] in (16, 32, 64) and (cfg["variant"], cfg["min_part"]) in autotune.KERNEL_CANDIDATES
     rng = np.random.default_rng(3)
     frames = rng.integers(0, 255, (40, 32, 32)).astype(np.uint8)
     with smip.Stack(32, 32, 8, batch_frames="auto", dtype=np.uint8) as a, smip.Stack(32, 32, 8) as b:
@@ -168,6 +172,16 @@ def test_autotune_on_device(smip, tmp_path, monkeypatch):
         from conftest import rel_l2
 
         assert rel_l2(a.bispectrum(), b.bispectrum()) <= 1e-6
+    rng = np.random.default_rng(4)
+    frames = rng.integers(0, 4095, (70, 128, 96)).astype(np.uint16)
+    out = []
+    for variant, min_part in ((0, 0), (1, 0), (0, 1 << 30)):
+        with smip.Stack(96, 128, 24, batch_frames=64) as st:
+            st.set_kernel_config(variant, min_part)
+            st.push_frames(frames)
+            out.append(st.bispectrum())
+    assert np.array_equal(out[0], out[1])  # staging does not change the order of the sums
+    assert rel_l2(out[2], out[0]) <= 1e-6  # an unsplit last wave sums in another order
 
 
 @pytest.mark.gpu
