@@ -67,11 +67,20 @@ __device__ C* stockham(C* x, C* y, const GenPlan& p, int nl, int ls, const C* tw
         const int R = p.fac[f];
         const int LR = L / R;
         const int step = LR / Ns; // L / (Ns R)
+        const unsigned* mp = p.map ? p.map + f * L : nullptr;
         for (int idx = threadIdx.x; idx < nl * L; idx += blockDim.x) {
             const int line = idx / L, o = idx - line * L;
-            const int k = o % Ns, t = o / Ns;
-            const int q = t % R, j = (t / R) * Ns + k;
-            const int e0 = (k + q * Ns) * step; // < L
+            int j, e0;
+            if (mp) { // precomputed for this length: no divisions
+                const unsigned m = __ldg(mp + o);
+                j = (int)(m & 0xffffu);
+                e0 = (int)(m >> 16);
+            } else {
+                const int k = o % Ns, t = o / Ns;
+                const int q = t % R;
+                j = (t / R) * Ns + k;
+                e0 = (k + q * Ns) * step; // < L
+            }
             const C* X = x + line * ls + j;
             C acc = X[0];
             int e = 0;
@@ -326,22 +335,26 @@ __global__ void __launch_bounds__(256) gen_lines_d_kernel(double2* __restrict__ 
 // Blocking per launch, chosen so that a CTA's shared memory stays below
 // kGenSmem for every length up to kMaxSide.
 constexpr size_t kGenSmem = 200 * 1024;
+// Lines per CTA: as many as fit in about 64 KB of shared memory, so that
+// several CTAs share an SM and hide each other's shared-memory latency
+// (one CTA of 200 KB per SM left the schedulers idle more than half the time).
+constexpr long kGenTarget = 64 * 1024;
 
-static int row_block(int W) { return std::max(1, std::min(16, 4096 / W)); }
+static int row_block(int W) { return (int)std::max(1L, std::min(16L, (kGenTarget / (16L * W) - 1) / 2)); }
 static size_t row_smem(int W, int rb) { return sizeof(dfc) * (size_t)W * (1 + 2 * rb); }
 static int col_lines(int H)
 {
     const long per = (long)H * (2 * sizeof(dfc) + 2 * sizeof(float2)); // one more column
     const long fixed = (long)H * (sizeof(dfc) + 3 * sizeof(float2));
-    return (int)std::max(1L, std::min(8L, ((long)kGenSmem - fixed) / per));
+    return (int)std::max(1L, std::min(8L, (kGenTarget - fixed) / per));
 }
 static size_t col_smem(int H, int cl)
 {
     return (size_t)H * (sizeof(dfc) * (1 + 2 * cl) + sizeof(float2) * (3 + 2 * cl));
 }
-static int xrow_block(int W) { return std::max(1, std::min(16, 8192 / W)); }
+static int xrow_block(int W) { return (int)std::max(1L, std::min(16L, (kGenTarget / (8L * W) - 1) / 2)); }
 static size_t xrow_smem(int W, int rb) { return sizeof(float2) * (size_t)W * (1 + 2 * rb); }
-static int lines_block(int L) { return std::max(1, std::min(8, 4096 / L)); }
+static int lines_block(int L) { return (int)std::max(1L, std::min(8L, (kGenTarget / (16L * L) - 1) / 2)); }
 static size_t lines_smem(int L, int nlb) { return sizeof(double2) * (size_t)L * (1 + 2 * nlb); }
 
 template <typename K> static cudaError_t allow(K kern, size_t bytes)

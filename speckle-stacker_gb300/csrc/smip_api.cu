@@ -198,6 +198,18 @@ int make_gen_tw(int L, GenTw* t)
         tdf[k].h = t32[k];
         tdf[k].l = make_float2((float)(t64[k].x - (double)hx), (float)(t64[k].y - (double)hy));
     }
+    // the passes' index map (GenPlan::map): j | e0 << 16 per pass and output
+    const GenPlan p = make_gen_plan(L);
+    std::vector<unsigned> map((size_t)p.nf * L);
+    for (int f = 0, Ns = 1; f < p.nf; Ns *= p.fac[f], ++f) {
+        const int R = p.fac[f], step = L / (Ns * R);
+        for (int o = 0; o < L; ++o) {
+            const int k = o % Ns, t = o / Ns, q = t % R;
+            map[(size_t)f * L + o] = (unsigned)((t / R) * Ns + k) | ((unsigned)((k + q * Ns) * step) << 16);
+        }
+    }
+    CUDA_TRY(cudaMalloc(&t->map, sizeof(unsigned) * map.size()));
+    CUDA_TRY(cudaMemcpy(t->map, map.data(), sizeof(unsigned) * map.size(), cudaMemcpyHostToDevice));
     CUDA_TRY(cudaMalloc(&t->df, sizeof(dfc) * L));
     CUDA_TRY(cudaMalloc(&t->f32, sizeof(float2) * L));
     CUDA_TRY(cudaMalloc(&t->f64, sizeof(double2) * L));
@@ -212,6 +224,7 @@ void free_gen_tw(GenTw* t)
     if (t->df) cudaFree(t->df);
     if (t->f32) cudaFree(t->f32);
     if (t->f64) cudaFree(t->f64);
+    if (t->map) cudaFree(t->map);
     *t = GenTw();
 }
 
@@ -564,6 +577,8 @@ struct smip_stack {
                 rc = make_gen_tw(g.H, &twH);
             if (rc)
                 return rc;
+            g.pW.map = twW.map;
+            g.pH.map = twH.map;
         }
         CUDA_TRY(cudaMalloc(&R, sizeof(float2) * half_elems()));
         CUDA_TRY(cudaMalloc(&corr, sizeof(float) * frame_elems() * Bf));

@@ -26,6 +26,9 @@ struct GenPlan {
     int L;
     int nf;
     int fac[kMaxFactors];
+    // per pass f and output o: j | e0 << 16, the pass's input index and twiddle
+    // exponent step (k_fftg.cu), nf x L entries in device memory (null: computed)
+    const unsigned* map = nullptr;
 };
 GenPlan make_gen_plan(int L);
 constexpr int kRowBlock = 16;     // rows per CTA in the row passes
@@ -55,6 +58,7 @@ struct GenTw {
     dfc* df = nullptr;
     float2* f32 = nullptr;
     double2* f64 = nullptr;
+    unsigned* map = nullptr; // GenPlan::map of this length
 };
 
 // Every kernel launch site reports itself here (process-wide counter).
