@@ -478,6 +478,7 @@ struct smip_stack {
     // batch runs on the copy stream cst while the kernels read the current one.
     void* stg[2] = { nullptr, nullptr };
     int cur = 0;                  // buffer being filled
+    size_t stg_bytes = 0;         // bytes per frame the two buffers hold (they only grow)
     cudaStream_t cst = nullptr;   // copy stream
     cudaEvent_t ev_copied[2] = { nullptr, nullptr }; // copies into stg[i] done (on cst)
     cudaEvent_t ev_free[2] = { nullptr, nullptr };   // kernels done reading stg[i] (on st)
@@ -490,7 +491,7 @@ struct smip_stack {
     const void* zc_src = nullptr;
     cudaEvent_t ev_zc = nullptr;
     double* spec_staging = nullptr; // spectra input (mode 2)
-    void* ref = nullptr;          // raw frame 0
+    void* ref = nullptr;          // raw frame 0 (room for 8 bytes per pixel, any frame type)
     double* ref_sq = nullptr;
     dfc* Gt = nullptr;            // row-FFT output, float-float
     float2 *T = nullptr, *S = nullptr, *R = nullptr;
@@ -586,8 +587,19 @@ struct smip_stack {
         CUDA_TRY(cudaMalloc(&ref_sq, sizeof(double)));
         CUDA_TRY(cudaMalloc(&err, sizeof(int)));
         CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), st));
-        return SMIP_OK;
+        // Everything a job needs is allocated here, with the stack, so that a
+        // pooled stack serves further jobs without allocating: an allocation
+        // (and a free, which synchronises the device) in the middle of
+        // serving stalls the request loop until the GPU drains.
+        CUDA_TRY(cudaMalloc(&ref, 8 * frame_elems()));
+        CUDA_TRY(cudaMalloc(&kscratch, bispec_scratch_bytes(ctx->num_sms)));
+        CUDA_TRY(cudaMalloc(&ktile_cnt, sizeof(int) * bispec_tile_counters(ctx->num_sms)));
+        CUDA_TRY(cudaMemsetAsync(ktile_cnt, 0, sizeof(int) * bispec_tile_counters(ctx->num_sms), st));
+        return ensure_shift_cap(kShiftCap0);
     }
+
+    // shifts of the first kShiftCap0 frames fit without growing the buffer
+    static constexpr long kShiftCap0 = 65536;
 
     int ensure_shift_cap(long n)
     {
@@ -605,14 +617,22 @@ struct smip_stack {
         return SMIP_OK;
     }
 
-    // the two frame buffers, the copy stream and its events (first frames)
+    // the two frame buffers, the copy stream and its events: made for the first
+    // frames, remade only for frames of a larger element type than the buffers
+    // hold (a smaller type reuses them)
     int ensure_staging(size_t fbytes)
     {
         if (!cst)
             CUDA_TRY(cudaStreamCreateWithFlags(&cst, cudaStreamNonBlocking));
+        if (stg[0] && stg_bytes < fbytes) { // larger frames: the buffers' last kernels must be done
+            CUDA_TRY(cudaStreamSynchronize(st));
+            free_staging();
+        }
         for (int i = 0; i < 2; ++i) {
-            if (!stg[i])
+            if (!stg[i]) {
                 CUDA_TRY(cudaMalloc(&stg[i], fbytes * Bf));
+                stg_bytes = fbytes;
+            }
             if (!ev_copied[i])
                 CUDA_TRY(cudaEventCreateWithFlags(&ev_copied[i], cudaEventDisableTiming));
             if (!ev_free[i])
@@ -632,6 +652,7 @@ struct smip_stack {
             free_rec[i] = false;
         }
         cur = 0;
+        stg_bytes = 0;
     }
 
     // Host-side preparation of the pending batch: every allocation and
@@ -644,11 +665,6 @@ struct smip_stack {
             int rc = ensure_shift_cap(nframes);
             if (rc)
                 return rc;
-        }
-        if (!kscratch) {
-            CUDA_TRY(cudaMalloc(&kscratch, bispec_scratch_bytes(ctx->num_sms)));
-            CUDA_TRY(cudaMalloc(&ktile_cnt, sizeof(int) * bispec_tile_counters(ctx->num_sms)));
-            CUDA_TRY(cudaMemsetAsync(ktile_cnt, 0, sizeof(int) * bispec_tile_counters(ctx->num_sms), st));
         }
         return SMIP_OK;
     }
@@ -870,11 +886,7 @@ extern "C" int smip_stack_push_frames(smip_stack_t s, const void* frames, int dt
     if (s->dtype >= 0 && s->dtype != dtype) {
         if (s->nframes != 0)
             return fail(SMIP_E_INVALID_ARGUMENT, "frame dtype differs from the stack's first frames");
-        CUDA_TRY(cudaStreamSynchronize(s->st)); // after a reset: new element type
-        s->free_staging();
-        cudaFree(s->ref);
-        s->ref = nullptr;
-        s->dtype = -1;
+        s->dtype = -1; // after a reset: a new element type (ensure_staging keeps big enough buffers)
     }
     const size_t fbytes = es * s->frame_elems();
     if (stride_bytes == 0)
@@ -884,7 +896,6 @@ extern "C" int smip_stack_push_frames(smip_stack_t s, const void* frames, int dt
     if (s->dtype < 0) {
         if ((rc = s->ensure_staging(fbytes)))
             return rc;
-        CUDA_TRY(cudaMalloc(&s->ref, fbytes));
         s->dtype = dtype;
     }
     s->mode = 1;
@@ -1413,18 +1424,10 @@ extern "C" int smip_stack_share_reference(smip_stack_t dst, smip_stack_t src)
     if (src->nframes != 0)
         return fail(SMIP_E_BAD_CALL, "src already holds frames");
     const size_t fbytes = dtype_size(dst->dtype) * dst->frame_elems();
-    if (src->dtype >= 0 && src->dtype != dst->dtype) { // buffers sized for another element type
-        CUDA_TRY(cudaStreamSynchronize(src->st));
-        src->free_staging();
-        cudaFree(src->ref);
-        src->ref = nullptr;
-    }
     src->dtype = dst->dtype;
     src->mode = 1;
     if (int rc2 = src->ensure_staging(fbytes))
         return rc2;
-    if (!src->ref)
-        CUDA_TRY(cudaMalloc(&src->ref, fbytes));
     CUDA_TRY(cudaMemcpy(src->ref, dst->ref, fbytes, cudaMemcpyDeviceToDevice));
     CUDA_TRY(cudaMemcpy(src->R, dst->R, sizeof(float2) * dst->half_elems(), cudaMemcpyDeviceToDevice));
     CUDA_TRY(cudaMemcpy(src->ref_sq, dst->ref_sq, sizeof(double), cudaMemcpyDeviceToDevice));
@@ -1591,20 +1594,8 @@ extern "C" int smip_stack_load_state(smip_stack_t s, const char* path)
     if (!rc) rc = file_to_dev(f, s->P, sizeof(double) * he);
     if (!rc) rc = file_to_dev(f, s->sum, 8 * fe);
     if (!rc && mode == 1) {
-        if (s->dtype >= 0 && s->dtype != dtype) { // buffers sized for another element type
-            s->free_staging();
-            cudaFree(s->ref);
-            s->ref = nullptr;
-            s->dtype = -1;
-        }
-        if (s->dtype < 0) {
-            if ((rc = s->ensure_staging(dtype_size(dtype) * fe)) == SMIP_OK) {
-                if (cudaMalloc(&s->ref, dtype_size(dtype) * fe) != cudaSuccess)
-                    rc = fail(SMIP_E_NO_MEMORY, "cudaMalloc failed");
-                else
-                    s->dtype = dtype;
-            }
-        }
+        if ((rc = s->ensure_staging(dtype_size(dtype) * fe)) == SMIP_OK)
+            s->dtype = dtype;
         if (!rc) rc = s->ensure_shift_cap(cnt[0]);
         if (!rc) rc = file_to_dev(f, s->shifts, sizeof(int) * 2 * (size_t)cnt[0]);
         if (!rc) rc = file_to_dev(f, s->ref, dtype_size(dtype) * fe);
