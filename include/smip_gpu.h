@@ -144,6 +144,13 @@ SMIP_GPU_API int smip_stack_sync(smip_stack_t s);
  * smip-cli run (main.cpp:281-312); the serving loop uses it. */
 SMIP_GPU_API int smip_batch_launch(smip_stack_t* stacks, long count);
 
+/* smip_batch_launch with reserve_sms streaming multiprocessors left out of
+ * the persistent grid (0 <= reserve_sms < SM count; 0 is smip_batch_launch),
+ * so that phase recoveries of stacks launched earlier -- one block each, on
+ * their high-priority streams -- run beside the launch instead of after it.
+ * One graph is kept per grid size.  Results do not depend on reserve_sms. */
+SMIP_GPU_API int smip_batch_launch_reserve(smip_stack_t* stacks, long count, int reserve_sms);
+
 /* Diagnostic of the failure path: runs a kernel whose two waits (an mbarrier
  * nothing arrives on, a device flag nothing sets) can never be satisfied.
  * Both give up after timeout_s seconds (at most 10), record the expiry and

@@ -86,7 +86,8 @@ struct DeviceCtx {
         int2* d_items = nullptr;
         int* d_ctrl = nullptr;
         size_t rec_cap = 0, item_cap = 0;
-        cudaGraphExec_t exec = nullptr;
+        cudaGraphExec_t exec = nullptr; // the graph for grid CTAs
+        int grid = 0;
         cudaEvent_t ev_used = nullptr; // the slot's last launch has read its host buffers
         bool used = false;
     };
@@ -1109,6 +1110,11 @@ static int multi_slot_reserve(DeviceCtx::MultiSlot& m, size_t nrec, size_t nitem
 
 extern "C" int smip_batch_launch(smip_stack_t* stacks, long count)
 {
+    return smip_batch_launch_reserve(stacks, count, 0);
+}
+
+extern "C" int smip_batch_launch_reserve(smip_stack_t* stacks, long count, int reserve_sms)
+{
     if (count < 0 || (count > 0 && !stacks))
         return fail(SMIP_E_INVALID_ARGUMENT, "invalid stack list");
     std::vector<smip_stack*> L;
@@ -1126,6 +1132,9 @@ extern "C" int smip_batch_launch(smip_stack_t* stacks, long count)
     if (L.empty())
         return SMIP_OK;
     DeviceCtx* ctx = L[0]->ctx;
+    if (reserve_sms < 0 || reserve_sms >= ctx->num_sms)
+        return fail(SMIP_E_INVALID_ARGUMENT, "reserve_sms must be in [0, SM count)");
+    const int grid = ctx->num_sms - reserve_sms;
     std::lock_guard<std::mutex> lk(*ctx->gmu);
     CUDA_TRY(cudaSetDevice(L[0]->device));
     if (!ctx->mst) {
@@ -1184,6 +1193,11 @@ extern "C" int smip_batch_launch(smip_stack_t* stacks, long count)
     // 3. the slot's graph on the batch stream, after every stack's per-frame kernels
     for (smip_stack* s : L)
         CUDA_TRY(cudaStreamWaitEvent(ctx->mst, s->ev_dep, 0));
+    if (m.exec && m.grid != grid) { // another grid size: capture again
+        CUDA_TRY(cudaEventSynchronize(m.ev_used));
+        cudaGraphExecDestroy(m.exec);
+        m.exec = nullptr;
+    }
     if (!m.exec) {
         cudaGraph_t graph = nullptr;
         CUDA_TRY(cudaStreamBeginCapture(ctx->mst, cudaStreamCaptureModeRelaxed));
@@ -1193,7 +1207,7 @@ extern "C" int smip_batch_launch(smip_stack_t* stacks, long count)
         if (ce == cudaSuccess)
             ce = cudaMemcpyAsync(m.d_ctrl, m.h_ctrl, 2 * sizeof(int), cudaMemcpyHostToDevice, ctx->mst);
         if (ce == cudaSuccess)
-            ce = launch_bispec_multi(m.d_recs, m.d_items, m.d_ctrl, ctx->num_sms, ctx->mst);
+            ce = launch_bispec_multi(m.d_recs, m.d_items, m.d_ctrl, grid, ctx->mst);
         const cudaError_t ee = cudaStreamEndCapture(ctx->mst, &graph);
         if (ce == cudaSuccess && ee == cudaSuccess)
             ce = cudaGraphInstantiate(&m.exec, graph, 0);
@@ -1204,6 +1218,7 @@ extern "C" int smip_batch_launch(smip_stack_t* stacks, long count)
             m.exec = nullptr;
             return fail(SMIP_E_CUDA, cudaGetErrorString(ce != cudaSuccess ? ce : ee));
         }
+        m.grid = grid;
     }
     CUDA_TRY(cudaGraphLaunch(m.exec, ctx->mst));
     CUDA_TRY(cudaEventRecord(m.ev_used, ctx->mst));

@@ -105,6 +105,7 @@ def _load():
         "smip_stack_merge": ([vp, vp], C.c_int),
         "smip_stack_set_kernel_config": ([vp, C.c_int, C.c_int], C.c_int),
         "smip_batch_launch": ([C.POINTER(vp), C.c_long], C.c_int),
+        "smip_batch_launch_reserve": ([C.POINTER(vp), C.c_long, C.c_int], C.c_int),
         "smip_diag_bounded_wait": ([C.c_int, C.c_double], C.c_int),
         "smip_stack_set_bispectrum": ([vp, fp, C.c_long], C.c_int),
         "smip_stack_save_state": ([vp, C.c_char_p], C.c_int),
@@ -161,14 +162,16 @@ def version():
     return a.value, b.value, c.value
 
 
-def batch_launch(stacks) -> None:
+def batch_launch(stacks, reserve_sms: int = 0) -> None:
     """Runs the pending frame batches of ``stacks``: each stack's per-frame
     kernels on its own stream, then the bispectrum work of all of them as one
-    persistent launch (a CUDA graph captured once); stacks without pending
-    frames are skipped.  Later calls on each stack are ordered after it."""
+    persistent launch (a CUDA graph captured once per grid size); stacks
+    without pending frames are skipped.  Later calls on each stack are ordered
+    after it.  reserve_sms: streaming multiprocessors left out of the
+    persistent grid, for the phase recoveries of earlier stacks."""
     stacks = list(stacks)
     arr = (C.c_void_p * max(1, len(stacks)))(*[st._h.value for st in stacks])
-    _check(_L().smip_batch_launch(arr, len(stacks)))
+    _check(_L().smip_batch_launch_reserve(arr, len(stacks), int(reserve_sms)))
 
 
 def diag_bounded_wait(device: int = 0, timeout_s: float = 0.05) -> None:

@@ -138,7 +138,11 @@ class Engine:
     graph: the last batches of the jobs whose frames are all in after a round
         run together (smip_gb300.batch_launch: their bispectrum work as one
         persistent launch from a captured CUDA graph) before their
-        reconstructions start, instead of one flush per job.
+        reconstructions start, instead of one flush per job.  The jobs of a
+        round go in groups of ``graph_group`` (largest frames first), each
+        group's reconstructions submitted right after its launch; while
+        reconstructions are in flight a launch leaves ``graph_reserve`` SMs
+        out of its grid, so that they run beside it.
     stall_timeout: seconds a streaming job may go without new frames from its
         producer before it fails (None: wait for ever).
     reco_mode: "spiral" (the reference's phase recovery, default) or "rings"
@@ -151,7 +155,8 @@ class Engine:
     def __init__(self, device: int = 0, budget_bytes: float = 120e9, max_active: int = 64, workers: int = 32,
                  stack_factory: Optional[Callable] = None, graph: bool = False,
                  batch_launch: Optional[Callable] = None, stall_timeout: Optional[float] = None,
-                 reco_mode: str = "spiral", chunks_per_round: int = 8):
+                 reco_mode: str = "spiral", chunks_per_round: int = 8, graph_group: int = 8,
+                 graph_reserve: int = 16):
         if stack_factory is None:
             from smip_gb300 import Stack
 
@@ -168,6 +173,8 @@ class Engine:
         self.stall_timeout = stall_timeout
         self.reco_mode = reco_mode
         self.chunks_per_round = max(1, int(chunks_per_round))
+        self.graph_group = max(1, int(graph_group))
+        self.graph_reserve = max(0, int(graph_reserve))
         self.pool: Dict[Tuple[int, int, int], list] = {}
         self.peak_bytes = 0.0
         self.peak_active = 0
@@ -295,11 +302,16 @@ class Engine:
                     elif entry[2] == len(job.frames):
                         active.remove(entry)
                         ready.append(entry)
-                if self.graph and ready:
-                    self.batch_launch([e[1] for e in ready])
-                for entry in ready:
-                    fut = ex.submit(self._finish, entry[0], entry[1], t0, entry[3])
-                    running[fut] = (entry[0], entry[1], entry[4], entry[3])
+                groups = [ready]
+                if self.graph and ready:  # longest reconstructions (largest frames) first
+                    ready.sort(key=lambda e: -e[0].shape[0] * e[0].shape[1])
+                    groups = [ready[i:i + self.graph_group] for i in range(0, len(ready), self.graph_group)]
+                for grp in groups:
+                    if self.graph:
+                        self.batch_launch([e[1] for e in grp], reserve_sms=self.graph_reserve if running else 0)
+                    for entry in grp:
+                        fut = ex.submit(self._finish, entry[0], entry[1], t0, entry[3])
+                        running[fut] = (entry[0], entry[1], entry[4], entry[3])
                 # completions
                 done = [f for f in running if f.done()]
                 for f in done:

@@ -76,14 +76,17 @@ def test_engine_graph_mode_launches_each_finished_job_once():
     jobs = _jobs(12)
     calls = []
 
-    def launch(stacks):
+    def launch(stacks, reserve_sms=0):
         assert all(len(st.frames) for st in stacks)  # every one holds its job's frames
-        calls.append([id(st) for st in stacks])
+        calls.append(([id(st) for st in stacks], reserve_sms))
 
-    eng = serve.Engine(max_active=5, workers=2, stack_factory=FakeStack, graph=True, batch_launch=launch)
+    eng = serve.Engine(max_active=5, workers=2, stack_factory=FakeStack, graph=True, batch_launch=launch,
+                       graph_group=2, graph_reserve=7)
     res, _ = eng.run(jobs, realtime=False)
     assert sorted(r.id for r in res) == list(range(12))
-    assert sum(len(c) for c in calls) == 12 and all(len(set(c)) == len(c) for c in calls)
+    assert sum(len(c) for c, _ in calls) == 12 and all(len(set(c)) == len(c) <= 2 for c, _ in calls)
+    # the first launch has no reconstruction beside it; a group after the first in a round has
+    assert calls[0][1] == 0 and calls[1][1] == 7 and {r for _, r in calls} <= {0, 7}
 
 
 def test_engine_realtime_respects_arrivals():
@@ -206,8 +209,8 @@ def test_batch_launch_matches_flush(smip):
             for st, fr in zip(stacks, frames):
                 st.reset()
                 st.push_frames(fr[rnd:])  # 64 frames run as a batch during the push
-            if graph:
-                smip.batch_launch(stacks)
+            if graph:  # the second round leaves 40 SMs out of the persistent grid
+                smip.batch_launch(stacks, reserve_sms=40 if rnd == 1 else 0)
             out.append([results(st) for st in stacks])
         for st in stacks:
             st.close()
@@ -218,9 +221,12 @@ def test_batch_launch_matches_flush(smip):
         for a, b in zip(re, rg):
             for x, y in zip(a, b):
                 assert np.array_equal(x, y)
-    with smip.Stack(64, 64, 16) as st, pytest.raises(smip.InvalidArgument):
+    with smip.Stack(64, 64, 16) as st:
         st.push_frames(frames[0][:3])
-        smip.batch_launch([st, st])
+        with pytest.raises(smip.InvalidArgument):
+            smip.batch_launch([st, st])
+        with pytest.raises(smip.InvalidArgument, match="reserve_sms"):
+            smip.batch_launch([st], reserve_sms=100000)
 
 
 class FailingStack(FakeStack):
