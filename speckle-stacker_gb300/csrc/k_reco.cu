@@ -26,6 +26,8 @@
 // cancellation; the mean, |mean| (consistency) and the stored phase are FP64.
 // B is read through a device replica of Bispectrum::get_element's index
 // arithmetic, aliasing included.
+#include <type_traits>
+
 #include "smip_dev.cuh"
 
 namespace smip_gpu {
@@ -207,24 +209,46 @@ __global__ void __launch_bounds__(256) reco_rlist_kernel(const RecoJob* __restri
     }
 }
 
-// The walk, one CTA per job.  Warp 0 runs the visits in order: for visit q it
-// waits for the share of the non-recent pairs, adds the recent pairs (or all
-// pairs when the list overflowed), forms the phase and advances `progress`.
-// Warps 1..15 form the non-recent shares of visits q = warp-1 (mod 15), each
-// once progress >= q - kRecoLag, into a ring of kRing slots.  Every wait is
+// The walk, one thread-block cluster per job.  Warp 0 of the cluster's rank-0
+// CTA runs the visits in order: for visit q it waits for the share of the
+// non-recent pairs, adds the recent pairs (or all pairs when the list
+// overflowed), forms the phase and advances `progress`.  The warps of the
+// other CTAs form the non-recent shares of visits q = g (mod number of such
+// warps), each once progress >= q - kRecoLag, and store them into a ring of
+// kRing slots in rank 0's shared memory.  A visit's share is split into up to
+// kMaxParts parts over ranges of its pair slots, summed by different warps
+// (only the kRecoLag visits ahead of the walk can be summed at any time, so
+// a visit's latency, not the warp count, sets the rate), and the serial warp
+// adds the parts in part order (distributed shared memory: st.async stores that complete
+// the slot's mbarrier, on which the serial warp waits locally).  `progress`
+// is published with a release at cluster scope, so the summing warps, after
+// their acquire, read the phases and flags the walk set from the phase map in
+// global memory, where an unflagged point holds NaN.  Rank 0 keeps its SM
+// for the serial warp (summing warps beside it take its issue slots: 3.4k
+// against 2.3k cycles per visit at 256 x 256, d = 32); a cluster of one CTA
+// (where the GPU cannot place more) sums on its other warps.  Every wait is
 // bounded; on a timeout the walk stops and the error is recorded.
 constexpr int kRing = 64;
 constexpr int kPhaseCache = 2048;
+constexpr int kWalkCtas = 8; // CTAs per job (cluster size), fewer where the GPU cannot place 8
+constexpr uint32_t kShareBytes = sizeof(float4) + sizeof(int); // one part's st.async payload
+constexpr int kMaxParts = 6;
+// static + the largest dynamic shared memory (1024 x 1024 flags, d = 64) fit a CTA's 227 KB
+static_assert(kRing * kMaxParts * (sizeof(float4) + sizeof(int)) + kRing * 8 + kPhaseCache * (sizeof(int) + sizeof(float2))
+                      + 64 + (sizeof(float2) + sizeof(int2)) * 65 * 65 + sizeof(unsigned) * (kMaxSide * kMaxSide / 32)
+                  <= 227 * 1024,
+              "walk shared memory");
+
+// parts per visit share: about 16 words of pair slots (512 slots) each
+__host__ __device__ __forceinline__ int share_parts(int nwords)
+{
+    const int p = nwords / 16;
+    return p < 1 ? 1 : (p > kMaxParts ? kMaxParts : p);
+}
 
 // CTA-scope acquire load / release store on shared memory: they order the
 // accesses after (before) them without waiting for this thread's other
 // outstanding loads, as a full fence would.
-__device__ __forceinline__ int ld_acquire_cta(const int* p)
-{
-    int v;
-    asm volatile("ld.acquire.cta.shared.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
-    return v;
-}
 __device__ __forceinline__ void st_release_cta(int* p, int v)
 {
     asm volatile("st.release.cta.shared.b32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
@@ -232,57 +256,67 @@ __device__ __forceinline__ void st_release_cta(int* p, int v)
 static_assert(kRing > kRecoLag + 1, "ring slots outlive the lag");
 constexpr unsigned long long kRecoWaitNs = 2000000000ull;
 
+__device__ __forceinline__ bool unflagged(float2 ph) { return isnan(ph.x); }
+
 __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJob* __restrict__ jobs)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ float4 ring_s[kRing];
-    __shared__ int ring_n[kRing];
-    __shared__ int ring_tag[kRing];
+    __shared__ float4 ring_s[kRing][kMaxParts];
+    __shared__ int ring_n[kRing][kMaxParts];
+    __shared__ __align__(8) uint64_t ring_bar[kRing]; // slot q % kRing: visit q's share has landed
     __shared__ int progress;
     __shared__ int abort_walk;
     __shared__ int pc_key[kPhaseCache];   // serial warp: phases it set, by point
     __shared__ float2 pc_val[kPhaseCache];
-    const RecoJob J = jobs[blockIdx.x];
+    const uint32_t rank = cluster_rank(), ncta = cluster_size();
+    const RecoJob J = jobs[blockIdx.x / ncta];
     const int W = J.W, H = J.H, De = J.De;
     const int nbits = W * H;
     const int nside = De + 1, nv = nside * nside, nwords = (nv + 31) / 32;
-    float2* vtab = reinterpret_cast<float2*>(smraw);                        // [nv] phases of the v disc
+    const int nparts = share_parts(nwords);
+    float2* vtab = reinterpret_cast<float2*>(smraw);                        // [nv] phases of the v disc (rank 0)
     int2* slot_v = reinterpret_cast<int2*>(vtab + nv);                      // [nv] (vx | vy << 16, map index of v)
-    unsigned int* flagbits = reinterpret_cast<unsigned int*>(slot_v + nv);  // [W*H bits]
-    for (int i = threadIdx.x; i < (nbits + 31) / 32; i += blockDim.x)
-        flagbits[i] = 0u;
+    unsigned int* flagbits = reinterpret_cast<unsigned int*>(slot_v + nv);  // [W*H bits] (rank 0)
     for (int i = threadIdx.x; i < nv; i += blockDim.x) {
-        vtab[i] = make_float2(0.f, 0.f);
         const int vx = -De / 2 + i % nside, vy = -De / 2 + i / nside;
         slot_v[i] = make_int2((int)(((unsigned)vx & 0xffffu) | ((unsigned)vy << 16)), wrap_idx(vx, vy, W, H));
     }
-    for (int i = threadIdx.x; i < kRing; i += blockDim.x)
-        ring_tag[i] = -1;
-    if (threadIdx.x == 0) {
-        progress = 0;
-        abort_walk = 0;
+    if (rank == 0) {
+        for (int i = threadIdx.x; i < (nbits + 31) / 32; i += blockDim.x)
+            flagbits[i] = 0u;
+        for (int i = threadIdx.x; i < nv; i += blockDim.x)
+            vtab[i] = make_float2(0.f, 0.f);
+        if (threadIdx.x == 0) {
+            progress = 0;
+            abort_walk = 0;
+            for (int i = 0; i < kRing; ++i) // one arrival per phase: the serial warp's expect_tx
+                mbar_init(&ring_bar[i], 1);
+            fence_mbar_init();
+        }
+        __syncthreads();
+        if (threadIdx.x < 5) { // seeds (phasereco.h:42-54); all inside the v disc
+            const int sx[5] = { 0, 1, 0, -1, 0 }, sy[5] = { 0, 0, 1, 0, -1 };
+            const int p = wrap_idx(sx[threadIdx.x], sy[threadIdx.x], W, H);
+            const float im = threadIdx.x < 3 ? 0.f : -0.f;
+            J.phf[p] = make_float2(1.f, im);
+            J.sums[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+            J.cnt[p] = -1;
+            vtab[(sy[threadIdx.x] + De / 2) * nside + sx[threadIdx.x] + De / 2] = make_float2(1.f, im);
+            atomicOr(&flagbits[p >> 5], 1u << (p & 31));
+        }
     }
-    __syncthreads();
-    if (threadIdx.x < 5) { // seeds (phasereco.h:42-54); all inside the v disc
-        const int sx[5] = { 0, 1, 0, -1, 0 }, sy[5] = { 0, 0, 1, 0, -1 };
-        const int p = wrap_idx(sx[threadIdx.x], sy[threadIdx.x], W, H);
-        const float im = threadIdx.x < 3 ? 0.f : -0.f;
-        J.phf[p] = make_float2(1.f, im);
-        J.sums[p] = make_float4(0.f, 0.f, 0.f, 0.f);
-        J.cnt[p] = -1;
-        vtab[(sy[threadIdx.x] + De / 2) * nside + sx[threadIdx.x] + De / 2] = make_float2(1.f, im);
-        atomicOr(&flagbits[p >> 5], 1u << (p & 31));
-    }
-    __syncthreads();
+    cluster_sync_all(); // rank 0's ring, progress and the seeds are set
     const int pmin0 = -(W >> 1), pmin1 = -(H >> 1);
     const int pmax0 = -W / 2 + W - 1, pmax1 = -H / 2 + H - 1;
     const int szW = (W / 2) * 2 + 1, szH = (H / 2) * 2 + 1;
     const int umn0 = -(szW / 2), umx0 = szW - szW / 2 - 1, umn1 = -(szH / 2), umx1 = szH - szH / 2 - 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    volatile int* vabort = &abort_walk;
+    const uint32_t a_abort = dsmem_addr(&abort_walk, 0);
+    const uint32_t a_progress = dsmem_addr(&progress, 0);
 
     auto flag = [&](int p) { return ((flagbits[p >> 5] >> (p & 31)) & 1u) != 0u; };
-    // bounded wait on a shared-memory condition; false on a timeout (then the walk stops)
+    // bounded wait on a condition; false on a timeout or when another warp
+    // of the cluster gave up (then the walk stops)
     auto wait_until = [&](auto cond) {
         if (cond())
             return true;
@@ -291,55 +325,68 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
             for (int i = 0; i < 64; ++i)
                 if (cond())
                     return true;
-            if (*vabort)
+            if (dsmem_ld_relaxed(a_abort))
                 return false;
             if (globaltimer_ns() - t0 > kRecoWaitNs) {
                 record_error(J.err, SMIP_DEV_ERR_TIMEOUT);
-                *vabort = 1;
+                dsmem_st_relaxed(a_abort, 1);
                 return false;
             }
         }
     };
 
-    // Pairs of visit q, eight slots per lane at a time, so that the plan,
-    // flag and phase gathers overlap; skip_recent leaves the recent pairs
-    // out (the serial warp takes them); phase reads the phase map.
-    auto sum_pairs = [&](int q, int2 w, bool skip_recent, auto phase, float& sr, float& si, int& cnt) {
+    // Pairs of visit q, eight slots per lane at a time, so that the plan and
+    // phase gathers overlap.  skip_recent leaves the recent pairs out (the
+    // serial warp takes them).  LOCAL: the serial warp's view (flags and v
+    // phases in rank 0's shared memory, u phases from `phase`); otherwise
+    // flags and both phases from the phase map in global memory (NaN: no
+    // phase yet).
+    // Words [wb, we) of the visit's pair slots.
+    auto sum_pairs = [&](int q, int2 w, bool skip_recent, auto local, auto phase, int wb, int we, float& sr, float& si,
+                         int& cnt) {
+        constexpr bool LOCAL = decltype(local)::value;
         constexpr int kB = 8;
         const unsigned* rb = J.rbits + (long long)q * nwords;
         const float2* prow = J.plan + (long long)q * nv;
-        for (int i0 = 0; i0 < nwords; i0 += kB) {
-            float2 bh[kB], ph[kB];
-            int tt[kB];
+        for (int i0 = wb; i0 < we; i0 += kB) {
+            float2 bh[kB], ph[kB], pvv[kB];
             bool use[kB];
 #pragma unroll
             for (int k = 0; k < kB; ++k) {
                 const int t = lane + 32 * (i0 + k);
-                tt[k] = t;
-                use[k] = i0 + k < nwords && t < nv;
+                use[k] = i0 + k < we && t < nv;
                 // slot t's bit is bit `lane` of word i0 + k
                 if (skip_recent)
                     use[k] = use[k] && !((rb[i0 + k] >> lane) & 1u);
                 bh[k] = use[k] ? prow[t] : make_float2(0.f, 0.f);
-                if (use[k]) { // flags and the phase gather do not wait for the plan
+                if (use[k]) { // the flags and phase gathers do not wait for the plan
                     const int2 sv = slot_v[t];
                     const int vx = (int)(short)(sv.x & 0xffff), vy = sv.x >> 16;
                     const int ux = w.x - vx, uy = w.y - vy;
                     const bool inu = !(ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1);
                     const int pu = inu ? wrap_idx(ux, uy, W, H) : 0, pv = sv.y;
-                    use[k] = inu && flag(pu) && flag(pv);
-                    ph[k] = use[k] ? phase(pu) : make_float2(0.f, 0.f);
+                    if constexpr (LOCAL) {
+                        use[k] = inu && flag(pu) && flag(pv);
+                        ph[k] = use[k] ? phase(pu) : make_float2(0.f, 0.f);
+                        pvv[k] = vtab[t];
+                    } else {
+                        ph[k] = inu ? J.phf[pu] : make_float2(0.f, 0.f);
+                        pvv[k] = J.phf[pv];
+                        use[k] = inu;
+                    }
                 }
             }
 #pragma unroll
             for (int k = 0; k < kB; ++k) {
+                if constexpr (!LOCAL)
+                    use[k] = use[k] && !unflagged(ph[k]) && !unflagged(pvv[k]);
                 if (!use[k] || (bh[k].x == 0.f && bh[k].y == 0.f)) // the plan's zero: never contributes
                     continue;
                 if (isnan(bh[k].x)) {
                     record_error(J.err, SMIP_DEV_ERR_OUT_OF_RANGE);
                     continue;
                 }
-                const float2 p = cmul(cmul(ph[k], vtab[tt[k]]), make_float2(bh[k].x, -bh[k].y));
+                const float2 p = cmul(cmul(ph[k], pvv[k]), make_float2(bh[k].x, -bh[k].y));
                 const float r = rsqrtf(p.x * p.x + p.y * p.y);
                 sr += p.x * r;
                 si += p.y * r;
@@ -347,8 +394,10 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
             }
         }
     };
+    using Local = std::true_type;
+    using Global = std::false_type;
 
-    if (warp == 0) {
+    if (rank == 0 && warp == 0) {
         // ------------------------------------------------ serial warp
         // Visit data that does not depend on the walk is loaded ahead: the
         // visit, its recent-pair count and slots two visits ahead, their plan
@@ -382,6 +431,10 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
             a.ba = a.ta >= 0 ? prow[a.ta] : make_float2(0.f, 0.f);
             a.bb = a.tb >= 0 ? prow[a.tb] : make_float2(0.f, 0.f);
         };
+        // every slot expects its first visit's share (visits 0 .. kRing-1)
+        if (lane == 0)
+            for (int i = 0; i < kRing; ++i)
+                mbar_arrive_expect_tx(&ring_bar[i], kShareBytes * nparts);
         Ahead c0 {}, c1 {}, c2 {};
         load_meta(0, c0);
         load_plan(0, c0);
@@ -417,10 +470,18 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
             run = run && !flag(pw);
             run = run && (abs(w.x) + abs(w.y) > 1);                                   // phasereco.h:84
             run = run && !(w.x < umn0 || w.x > umx0 || w.y < umn1 || w.y > umx1);
+            // every visit's share lands (the summing warps do not know which
+            // visits run).  The slot is re-armed for visit q + kRing at once:
+            // its next share cannot land before progress passes q + kRing -
+            // kRecoLag, and an arrive here, before this visit's global stores,
+            // does not wait for them (an arrive is a release)
+            const int slot = q % kRing;
+            if (!__all_sync(0xffffffffu,
+                            wait_until([&] { return mbar_try_wait(&ring_bar[slot], (uint32_t)(q / kRing) & 1u); }) ? 1 : 0))
+                break;
+            if (lane == 0 && q + kRing < J.nvisits)
+                mbar_arrive_expect_tx(&ring_bar[slot], kShareBytes * nparts);
             if (run) {
-                const int slot = q % kRing;
-                if (!__all_sync(0xffffffffu, wait_until([&] { return ld_acquire_cta(&ring_tag[slot]) == q; }) ? 1 : 0))
-                    break;
                 float sr = 0.f, si = 0.f;
                 int cnt = 0;
                 if (c0.rc >= 0) {
@@ -429,7 +490,7 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
                     if (c0.tb >= 0)
                         term_s(c0.tb, c0.bb, w, sr, si, cnt);
                 } else {
-                    sum_pairs(q, w, false, phase_of, sr, si, cnt);
+                    sum_pairs(q, w, false, Local {}, phase_of, 0, nwords, sr, si, cnt);
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
@@ -438,12 +499,18 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
                     cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
                 }
                 if (lane == 0) {
-                    // float-float: the non-recent share plus the recent one
-                    const float4 o4 = ring_s[slot];
+                    // float-float: the non-recent share's parts in order, plus the recent one
+                    const float4 o4 = ring_s[slot][0];
                     float rh = o4.x, rl = o4.y, ih = o4.z, il = o4.w;
+                    cnt += ring_n[slot][0];
+                    for (int pp = 1; pp < nparts; ++pp) {
+                        const float4 op = ring_s[slot][pp];
+                        ff_add(rh, rl, op.x, op.y);
+                        ff_add(ih, il, op.z, op.w);
+                        cnt += ring_n[slot][pp];
+                    }
                     ff_add(rh, rl, sr, 0.f);
                     ff_add(ih, il, si, 0.f);
-                    cnt += ring_n[slot];
                     if (cnt > 0) {
                         // FP32 phase for the chain; FP64 values are formed after the walk
                         const float s2 = rh * rh + ih * ih;
@@ -465,18 +532,23 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
                 }
                 __syncwarp();
             }
-            // publish progress every 8 visits (a release store; the lag leaves
-            // the slack)
-            if (((q & 7) == 7 || q + 1 == J.nvisits) && lane == 0)
-                st_release_cta(&progress, q + 1);
+            // publish progress every 16 visits (a release store at cluster
+            // scope, which waits for this thread's stores to the phase map
+            // to reach every CTA; the lag leaves the slack)
+            if (((q & 15) == 15 || q + 1 == J.nvisits) && lane == 0)
+                dsmem_st_release(a_progress, q + 1);
             __syncwarp();
             c0 = c1;
             c1 = c2;
         }
     } else {
         // ------------------------------------------- non-recent shares
-        for (int q = warp - 1; q < J.nvisits; q += kRecoThreads / 32 - 1) {
-            if (!__all_sync(0xffffffffu, wait_until([&] { return ld_acquire_cta(&progress) >= q - kRecoLag; }) ? 1 : 0))
+        const int nsum = ncta > 1 ? (int)(ncta - 1) * (kRecoThreads / 32) : kRecoThreads / 32 - 1;
+        const int g = ncta > 1 ? (int)(rank - 1) * (kRecoThreads / 32) + warp : warp - 1;
+        const long long nitems = (long long)J.nvisits * nparts; // (visit, part), visits in order
+        for (long long it = (ncta > 1 && rank == 0) ? nitems : g; it < nitems; it += nsum) {
+            const int q = (int)(it / nparts), part = (int)(it - (long long)q * nparts);
+            if (!__all_sync(0xffffffffu, wait_until([&] { return dsmem_ld_acquire(a_progress) >= q - kRecoLag; }) ? 1 : 0))
                 break;
             const int2 w = J.visits[q];
             const int rc = J.rcount[q];
@@ -484,7 +556,8 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
             int cnt = 0;
             const bool inmap = !(w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1);
             if (rc >= 0 && inmap)
-                sum_pairs(q, w, true, [&](int pu) { return J.phf[pu]; }, sr, si, cnt);
+                sum_pairs(q, w, true, Global {}, 0, (int)((long long)part * nwords / nparts),
+                          (int)((long long)(part + 1) * nwords / nparts), sr, si, cnt);
             // float-float over the lanes, lane 0's order
             float rh = sr, rl = 0.f, ih = si, il = 0.f;
 #pragma unroll
@@ -497,14 +570,16 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
             }
             if (lane == 0) {
                 const int slot = q % kRing;
-                ring_s[slot] = make_float4(rh, rl, ih, il);
-                ring_n[slot] = cnt;
-                st_release_cta(&ring_tag[slot], q);
+                const uint32_t bar = dsmem_addr(&ring_bar[slot], 0);
+                dsmem_st_async_f4(dsmem_addr(&ring_s[slot][part], 0), make_float4(rh, rl, ih, il), bar);
+                dsmem_st_async_i(dsmem_addr(&ring_n[slot][part], 0), cnt, bar);
             }
             __syncwarp();
         }
     }
-    __syncthreads();
+    cluster_sync_all(); // no CTA reads or writes rank 0's shared memory after this
+    if (rank != 0)
+        return;
     // FP64 mean, consistency and phase of every point (phasereco.h:110-122),
     // and the flag map
     for (int p = threadIdx.x; p < nbits; p += blockDim.x) {
@@ -735,9 +810,32 @@ cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int
     cudaError_t e = cudaFuncSetAttribute(phase_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     if (e != cudaSuccess)
         return e;
-    phase_pipe_kernel<<<njobs, kRecoThreads, smem, st>>>(jobs_dev);
+    // one cluster per job: kWalkCtas CTAs, or the largest power of two below
+    // it that the GPU can place
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(kRecoThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int ncta = kWalkCtas;
+    for (; ncta > 1; ncta /= 2) {
+        attr[0].val.clusterDim.x = ncta;
+        cfg.gridDim = dim3(ncta);
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, phase_pipe_kernel, &cfg) == cudaSuccess && nclusters >= 1)
+            break;
+        cudaGetLastError();
+    }
+    attr[0].val.clusterDim.x = ncta;
+    cfg.gridDim = dim3(njobs * ncta);
+    e = cudaLaunchKernelEx(&cfg, phase_pipe_kernel, jobs_dev);
     note_launches(1);
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 } // namespace smip_gpu

@@ -387,7 +387,8 @@ struct Reco {
             R = radius;
         }
         CUDA_TRY(cudaMemsetAsync(phases, 0, sizeof(double2) * np, st));
-        CUDA_TRY(cudaMemsetAsync(phf, 0, sizeof(float2) * np, st));
+        // the spiral walk's phase map marks a point without a phase by NaN (all bits set)
+        CUDA_TRY(cudaMemsetAsync(phf, mode == 1 ? 0 : 0xff, sizeof(float2) * np, st));
         CUDA_TRY(cudaMemsetAsync(cons, 0, sizeof(double) * np, st));
         RecoJob j;
         j.B = Bnorm;

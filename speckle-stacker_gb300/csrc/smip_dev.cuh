@@ -461,6 +461,75 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     }
 }
 
+// ------------------------------------------- thread-block clusters (DSMEM)
+// A shared-memory variable of the CTA of rank `rank` in this CTA's cluster,
+// as a shared::cluster address (mapa); valid for this CTA's own rank too.
+__device__ __forceinline__ uint32_t dsmem_addr(const void* p, uint32_t rank)
+{
+    uint32_t a;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(a) : "r"(smem_u32(p)), "r"(rank));
+    return a;
+}
+__device__ __forceinline__ uint32_t cluster_rank()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t cluster_size()
+{
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+// acquire / release at cluster scope: pairs of them order the memory accesses
+// (global and shared) of threads in different CTAs of the cluster
+__device__ __forceinline__ int dsmem_ld_acquire(uint32_t a)
+{
+    int v;
+    asm volatile("ld.acquire.cluster.shared::cluster.b32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ int dsmem_ld_relaxed(uint32_t a)
+{
+    int v;
+    asm volatile("ld.relaxed.cluster.shared::cluster.b32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ void dsmem_st_release(uint32_t a, int v)
+{
+    asm volatile("st.release.cluster.shared::cluster.b32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void dsmem_st_relaxed(uint32_t a, int v)
+{
+    asm volatile("st.relaxed.cluster.shared::cluster.b32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void dsmem_st_f4(uint32_t a, float4 v)
+{
+    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+// Stores into another CTA's shared memory that complete a transaction count
+// on an mbarrier there (st.async): once the barrier's phase completes, a
+// thread of that CTA that waited on it sees the data.
+__device__ __forceinline__ void dsmem_st_async_f4(uint32_t a, float4 v, uint32_t bar)
+{
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.f32 [%0], {%1, %2, %3, %4}, [%5];" ::"r"(a),
+                 "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ void dsmem_st_async_i(uint32_t a, int v, uint32_t bar)
+{
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(a), "r"(v), "r"(bar)
+                 : "memory");
+}
+// all threads of the cluster; every CTA's shared memory stays valid until
+// all have arrived
+__device__ __forceinline__ void cluster_sync_all()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // 3-D tiled TMA load into shared memory, completion signalled on bar.
 __device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, int x, int y, int z, uint64_t* bar)
 {
