@@ -9,15 +9,18 @@
 // serial chain.  Most of a point's pairs, though, read phases that were final
 // long before: a pair is "recent" only when u or v was visited within the
 // kRecoLag visits before w (the arc of the ring just behind w).  The walk is
-// therefore split (one CTA per job):
-//   - warps 1..15 form, for visit q, the sum over its non-recent pairs as soon
-//     as the walk has passed q - kRecoLag, eight pair slots per lane at a time
-//     so that the plan, flag and phase gathers overlap;
-//   - warp 0 runs the visits in order and adds only the recent pairs (a list
+// therefore split:
+//   - summing warps form, for visit q, the sum over its non-recent pairs as
+//     soon as the walk has passed q - kRecoLag, eight pair slots per lane at a
+//     time so that the plan, flag and phase gathers overlap;
+//   - one serial warp runs the visits in order and adds only the recent pairs (a list
 //     of at most kRecentMax per visit, prefetched with the plan phasors) to
 //     that share, then sets the point's phase and flag.
 // Which pairs are recent depends only on the visit list (per point: its visit
 // indices), so it is computed in parallel before the walk.
+// Depths below kClusterDepth walk in one CTA (phase_pipe_kernel); deeper
+// bispectra, whose (d+1)^2 pairs per visit one CTA's summing warps cannot
+// keep up with, walk in a thread-block cluster (phase_cluster_kernel).
 //
 // Precision: per-pair products in FP32 from an FP32 mirror of the phase map
 // (~1e-7 rad per pair); the non-recent share is summed in FP32 per lane and in
@@ -230,7 +233,13 @@ __global__ void __launch_bounds__(256) reco_rlist_kernel(const RecoJob* __restri
 // bounded; on a timeout the walk stops and the error is recorded.
 constexpr int kRing = 64;
 constexpr int kPhaseCache = 2048;
-constexpr int kWalkCtas = 8; // CTAs per job (cluster size), fewer where the GPU cannot place 8
+// CTAs per job (cluster size) from depth kClusterDepth on, fewer where the GPU
+// cannot place 8.  Below it phase_pipe_kernel walks in one CTA: its summing
+// warps keep up with the serial warp (256 x 256, d = 32, R = 128: 58.0 ms in
+// one CTA, 59.4 ms in a cluster), and a cluster would hold 8 SMs instead of 1
+// while it walks, which other jobs sharing the GPU need.
+constexpr int kWalkCtas = 8;
+constexpr int kClusterDepth = 40;
 constexpr uint32_t kShareBytes = sizeof(float4) + sizeof(int); // one part's st.async payload
 constexpr int kMaxParts = 6;
 // static + the largest dynamic shared memory (1024 x 1024 flags, d = 64) fit a CTA's 227 KB
@@ -258,7 +267,7 @@ constexpr unsigned long long kRecoWaitNs = 2000000000ull;
 
 __device__ __forceinline__ bool unflagged(float2 ph) { return isnan(ph.x); }
 
-__global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJob* __restrict__ jobs)
+__global__ void __launch_bounds__(kRecoThreads, 1) phase_cluster_kernel(const RecoJob* __restrict__ jobs)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ float4 ring_s[kRing][kMaxParts];
@@ -603,6 +612,319 @@ __global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJ
     }
 }
 
+// The walk in one CTA per job (depths below kClusterDepth).  Warp 0 runs the visits in order: for visit q it
+// waits for the share of the non-recent pairs, adds the recent pairs (or all
+// pairs when the list overflowed), forms the phase and advances `progress`.
+// Warps 1..15 form the non-recent shares of visits q = warp-1 (mod 15), each
+// once progress >= q - kRecoLag, into a ring of kRing slots.  Every wait is
+// bounded; on a timeout the walk stops and the error is recorded.
+
+// CTA-scope acquire load / release store on shared memory: they order the
+// accesses after (before) them without waiting for this thread's other
+// outstanding loads, as a full fence would.
+__device__ __forceinline__ int ld_acquire_cta(const int* p)
+{
+    int v;
+    asm volatile("ld.acquire.cta.shared.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+    return v;
+}
+
+__global__ void __launch_bounds__(kRecoThreads, 1) phase_pipe_kernel(const RecoJob* __restrict__ jobs)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ float4 ring_s[kRing];
+    __shared__ int ring_n[kRing];
+    __shared__ int ring_tag[kRing];
+    __shared__ int progress;
+    __shared__ int abort_walk;
+    __shared__ int pc_key[kPhaseCache];   // serial warp: phases it set, by point
+    __shared__ float2 pc_val[kPhaseCache];
+    const RecoJob J = jobs[blockIdx.x];
+    const int W = J.W, H = J.H, De = J.De;
+    const int nbits = W * H;
+    const int nside = De + 1, nv = nside * nside, nwords = (nv + 31) / 32;
+    float2* vtab = reinterpret_cast<float2*>(smraw);                        // [nv] phases of the v disc
+    int2* slot_v = reinterpret_cast<int2*>(vtab + nv);                      // [nv] (vx | vy << 16, map index of v)
+    unsigned int* flagbits = reinterpret_cast<unsigned int*>(slot_v + nv);  // [W*H bits]
+    for (int i = threadIdx.x; i < (nbits + 31) / 32; i += blockDim.x)
+        flagbits[i] = 0u;
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+        vtab[i] = make_float2(0.f, 0.f);
+        const int vx = -De / 2 + i % nside, vy = -De / 2 + i / nside;
+        slot_v[i] = make_int2((int)(((unsigned)vx & 0xffffu) | ((unsigned)vy << 16)), wrap_idx(vx, vy, W, H));
+    }
+    for (int i = threadIdx.x; i < kRing; i += blockDim.x)
+        ring_tag[i] = -1;
+    if (threadIdx.x == 0) {
+        progress = 0;
+        abort_walk = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x < 5) { // seeds (phasereco.h:42-54); all inside the v disc
+        const int sx[5] = { 0, 1, 0, -1, 0 }, sy[5] = { 0, 0, 1, 0, -1 };
+        const int p = wrap_idx(sx[threadIdx.x], sy[threadIdx.x], W, H);
+        const float im = threadIdx.x < 3 ? 0.f : -0.f;
+        J.phf[p] = make_float2(1.f, im);
+        J.sums[p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        J.cnt[p] = -1;
+        vtab[(sy[threadIdx.x] + De / 2) * nside + sx[threadIdx.x] + De / 2] = make_float2(1.f, im);
+        atomicOr(&flagbits[p >> 5], 1u << (p & 31));
+    }
+    __syncthreads();
+    const int pmin0 = -(W >> 1), pmin1 = -(H >> 1);
+    const int pmax0 = -W / 2 + W - 1, pmax1 = -H / 2 + H - 1;
+    const int szW = (W / 2) * 2 + 1, szH = (H / 2) * 2 + 1;
+    const int umn0 = -(szW / 2), umx0 = szW - szW / 2 - 1, umn1 = -(szH / 2), umx1 = szH - szH / 2 - 1;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    volatile int* vabort = &abort_walk;
+
+    auto flag = [&](int p) { return ((flagbits[p >> 5] >> (p & 31)) & 1u) != 0u; };
+    // bounded wait on a shared-memory condition; false on a timeout (then the walk stops)
+    auto wait_until = [&](auto cond) {
+        if (cond())
+            return true;
+        const unsigned long long t0 = globaltimer_ns();
+        for (;;) {
+            for (int i = 0; i < 64; ++i)
+                if (cond())
+                    return true;
+            if (*vabort)
+                return false;
+            if (globaltimer_ns() - t0 > kRecoWaitNs) {
+                record_error(J.err, SMIP_DEV_ERR_TIMEOUT);
+                *vabort = 1;
+                return false;
+            }
+        }
+    };
+
+    // Pairs of visit q, eight slots per lane at a time, so that the plan,
+    // flag and phase gathers overlap; skip_recent leaves the recent pairs
+    // out (the serial warp takes them); phase reads the phase map.
+    auto sum_pairs = [&](int q, int2 w, bool skip_recent, auto phase, float& sr, float& si, int& cnt) {
+        constexpr int kB = 8;
+        const unsigned* rb = J.rbits + (long long)q * nwords;
+        const float2* prow = J.plan + (long long)q * nv;
+        for (int i0 = 0; i0 < nwords; i0 += kB) {
+            float2 bh[kB], ph[kB];
+            int tt[kB];
+            bool use[kB];
+#pragma unroll
+            for (int k = 0; k < kB; ++k) {
+                const int t = lane + 32 * (i0 + k);
+                tt[k] = t;
+                use[k] = i0 + k < nwords && t < nv;
+                // slot t's bit is bit `lane` of word i0 + k
+                if (skip_recent)
+                    use[k] = use[k] && !((rb[i0 + k] >> lane) & 1u);
+                bh[k] = use[k] ? prow[t] : make_float2(0.f, 0.f);
+                if (use[k]) { // flags and the phase gather do not wait for the plan
+                    const int2 sv = slot_v[t];
+                    const int vx = (int)(short)(sv.x & 0xffff), vy = sv.x >> 16;
+                    const int ux = w.x - vx, uy = w.y - vy;
+                    const bool inu = !(ux < pmin0 || ux > pmax0 || uy < pmin1 || uy > pmax1);
+                    const int pu = inu ? wrap_idx(ux, uy, W, H) : 0, pv = sv.y;
+                    use[k] = inu && flag(pu) && flag(pv);
+                    ph[k] = use[k] ? phase(pu) : make_float2(0.f, 0.f);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kB; ++k) {
+                if (!use[k] || (bh[k].x == 0.f && bh[k].y == 0.f)) // the plan's zero: never contributes
+                    continue;
+                if (isnan(bh[k].x)) {
+                    record_error(J.err, SMIP_DEV_ERR_OUT_OF_RANGE);
+                    continue;
+                }
+                const float2 p = cmul(cmul(ph[k], vtab[tt[k]]), make_float2(bh[k].x, -bh[k].y));
+                const float r = rsqrtf(p.x * p.x + p.y * p.y);
+                sr += p.x * r;
+                si += p.y * r;
+                ++cnt;
+            }
+        }
+    };
+
+    if (warp == 0) {
+        // ------------------------------------------------ serial warp
+        // Visit data that does not depend on the walk is loaded ahead: the
+        // visit, its recent-pair count and slots two visits ahead, their plan
+        // phasors one visit ahead.  Phases the walk just set come from a
+        // shared-memory cache keyed by point (a miss reads the phase map).
+        for (int i = lane; i < kPhaseCache; i += 32)
+            pc_key[i] = -1;
+        __syncwarp();
+        struct Ahead {
+            int2 w;
+            int rc, ta, tb;
+            float2 ba, bb;
+        };
+        // the list slots are loaded without waiting for the count (a visit's
+        // kRecentMax entries are always allocated) and masked one visit later
+        auto load_meta = [&](int q, Ahead& a) {
+            if (q >= J.nvisits)
+                return;
+            a.w = J.visits[q];
+            a.rc = J.rcount[q];
+            const unsigned short* rl = J.rlist + (long long)q * kRecentMax;
+            a.ta = rl[lane];
+            a.tb = rl[lane + 32];
+        };
+        auto load_plan = [&](int q, Ahead& a) {
+            if (q >= J.nvisits)
+                return;
+            a.ta = lane < a.rc ? a.ta : -1;
+            a.tb = lane + 32 < a.rc ? a.tb : -1;
+            const float2* prow = J.plan + (long long)q * nv;
+            a.ba = a.ta >= 0 ? prow[a.ta] : make_float2(0.f, 0.f);
+            a.bb = a.tb >= 0 ? prow[a.tb] : make_float2(0.f, 0.f);
+        };
+        Ahead c0 {}, c1 {}, c2 {};
+        load_meta(0, c0);
+        load_plan(0, c0);
+        load_meta(1, c1);
+        auto phase_of = [&](int p) {
+            const int h = p & (kPhaseCache - 1);
+            return pc_key[h] == p ? pc_val[h] : J.phf[p];
+        };
+        auto term_s = [&](int t, float2 bh, int2 w, float& sr, float& si, int& cnt) {
+            if (bh.x == 0.f && bh.y == 0.f)
+                return;
+            const int2 sv = slot_v[t];
+            const int vx = (int)(short)(sv.x & 0xffff), vy = sv.x >> 16;
+            const int pu = wrap_idx(w.x - vx, w.y - vy, W, H), pv = sv.y;
+            if (!flag(pu) || !flag(pv))
+                return;
+            if (isnan(bh.x)) {
+                record_error(J.err, SMIP_DEV_ERR_OUT_OF_RANGE);
+                return;
+            }
+            const float2 ph = cmul(cmul(phase_of(pu), vtab[t]), make_float2(bh.x, -bh.y));
+            const float r = rsqrtf(ph.x * ph.x + ph.y * ph.y);
+            sr += ph.x * r;
+            si += ph.y * r;
+            ++cnt;
+        };
+        for (int q = 0; q < J.nvisits; ++q) {
+            load_plan(q + 1, c1); // its slots were loaded one visit ago
+            load_meta(q + 2, c2);
+            const int2 w = c0.w;
+            bool run = !(w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1);
+            const int pw = run ? wrap_idx(w.x, w.y, W, H) : 0;
+            run = run && !flag(pw);
+            run = run && (abs(w.x) + abs(w.y) > 1);                                   // phasereco.h:84
+            run = run && !(w.x < umn0 || w.x > umx0 || w.y < umn1 || w.y > umx1);
+            if (run) {
+                const int slot = q % kRing;
+                if (!__all_sync(0xffffffffu, wait_until([&] { return ld_acquire_cta(&ring_tag[slot]) == q; }) ? 1 : 0))
+                    break;
+                float sr = 0.f, si = 0.f;
+                int cnt = 0;
+                if (c0.rc >= 0) {
+                    if (c0.ta >= 0)
+                        term_s(c0.ta, c0.ba, w, sr, si, cnt);
+                    if (c0.tb >= 0)
+                        term_s(c0.tb, c0.bb, w, sr, si, cnt);
+                } else {
+                    sum_pairs(q, w, false, phase_of, sr, si, cnt);
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+                    si += __shfl_xor_sync(0xffffffffu, si, o);
+                    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+                }
+                if (lane == 0) {
+                    // float-float: the non-recent share plus the recent one
+                    const float4 o4 = ring_s[slot];
+                    float rh = o4.x, rl = o4.y, ih = o4.z, il = o4.w;
+                    ff_add(rh, rl, sr, 0.f);
+                    ff_add(ih, il, si, 0.f);
+                    cnt += ring_n[slot];
+                    if (cnt > 0) {
+                        // FP32 phase for the chain; FP64 values are formed after the walk
+                        const float s2 = rh * rh + ih * ih;
+                        const float lim = 2.220446049250313e-16f * (float)cnt;
+                        float2 pf = make_float2(0.f, 0.f);
+                        if (s2 > lim * lim) {
+                            const float r = rsqrtf(s2);
+                            pf = make_float2(rh * r, ih * r);
+                        }
+                        J.phf[pw] = pf;
+                        J.sums[pw] = make_float4(rh, rl, ih, il);
+                        J.cnt[pw] = cnt;
+                        if (abs(w.x) <= De / 2 && abs(w.y) <= De / 2)
+                            vtab[(w.y + De / 2) * nside + w.x + De / 2] = pf;
+                        pc_val[pw & (kPhaseCache - 1)] = pf;
+                        pc_key[pw & (kPhaseCache - 1)] = pw;
+                        flagbits[pw >> 5] |= 1u << (pw & 31);
+                    }
+                }
+                __syncwarp();
+            }
+            // publish progress every 8 visits (a release store; the lag leaves
+            // the slack)
+            if (((q & 7) == 7 || q + 1 == J.nvisits) && lane == 0)
+                st_release_cta(&progress, q + 1);
+            __syncwarp();
+            c0 = c1;
+            c1 = c2;
+        }
+    } else {
+        // ------------------------------------------- non-recent shares
+        for (int q = warp - 1; q < J.nvisits; q += kRecoThreads / 32 - 1) {
+            if (!__all_sync(0xffffffffu, wait_until([&] { return ld_acquire_cta(&progress) >= q - kRecoLag; }) ? 1 : 0))
+                break;
+            const int2 w = J.visits[q];
+            const int rc = J.rcount[q];
+            float sr = 0.f, si = 0.f;
+            int cnt = 0;
+            const bool inmap = !(w.x < pmin0 || w.x > pmax0 || w.y < pmin1 || w.y > pmax1);
+            if (rc >= 0 && inmap)
+                sum_pairs(q, w, true, [&](int pu) { return J.phf[pu]; }, sr, si, cnt);
+            // float-float over the lanes, lane 0's order
+            float rh = sr, rl = 0.f, ih = si, il = 0.f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
+                const float c = __shfl_xor_sync(0xffffffffu, ih, o), e = __shfl_xor_sync(0xffffffffu, il, o);
+                ff_add(rh, rl, a, b);
+                ff_add(ih, il, c, e);
+                cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+            }
+            if (lane == 0) {
+                const int slot = q % kRing;
+                ring_s[slot] = make_float4(rh, rl, ih, il);
+                ring_n[slot] = cnt;
+                st_release_cta(&ring_tag[slot], q);
+            }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    // FP64 mean, consistency and phase of every point (phasereco.h:110-122),
+    // and the flag map
+    for (int p = threadIdx.x; p < nbits; p += blockDim.x) {
+        const unsigned f = (flagbits[p >> 5] >> (p & 31)) & 1u;
+        J.flags[p] = f;
+        if (!f)
+            continue;
+        const int n = J.cnt[p];
+        if (n < 0) { // seed
+            J.phases[p] = make_double2(1.0, J.phf[p].y);
+            J.cons[p] = 1.0;
+            continue;
+        }
+        const float4 s = J.sums[p];
+        const double mr = ((double)s.x + (double)s.y) / (double)n;
+        const double mi = ((double)s.z + (double)s.w) / (double)n;
+        const double ab = sqrt(mr * mr + mi * mi);
+        J.cons[p] = ab;
+        J.phases[p] = ab > 2.220446049250313080847263336181640625e-16 ? make_double2(mr / ab, mi / ab)
+                                                                      : make_double2(0.0, 0.0);
+    }
+}
+
 // ------------------------------------------ ring-parallel estimator (opt-in)
 // A different estimator from the reference's spiral, offered as an option:
 // the spiral's visits are grouped by the radius r at which NextRecoIndex makes
@@ -807,7 +1129,15 @@ cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int
     // the static shared memory (ring, phase cache) counts against it too
     const size_t smem_max = (sizeof(float2) + sizeof(int2)) * 65 * 65
                             + sizeof(unsigned int) * (((size_t)kMaxSide * kMaxSide + 31) / 32);
-    cudaError_t e = cudaFuncSetAttribute(phase_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+    if (max_De < kClusterDepth) { // one CTA per job
+        cudaError_t e = cudaFuncSetAttribute(phase_pipe_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+        if (e != cudaSuccess)
+            return e;
+        phase_pipe_kernel<<<njobs, kRecoThreads, smem, st>>>(jobs_dev);
+        note_launches(1);
+        return cudaGetLastError();
+    }
+    cudaError_t e = cudaFuncSetAttribute(phase_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     if (e != cudaSuccess)
         return e;
     // one cluster per job: kWalkCtas CTAs, or the largest power of two below
@@ -827,13 +1157,13 @@ cudaError_t launch_phase_reco(const RecoJob* jobs_dev, int njobs, int max_W, int
         attr[0].val.clusterDim.x = ncta;
         cfg.gridDim = dim3(ncta);
         int nclusters = 0;
-        if (cudaOccupancyMaxActiveClusters(&nclusters, phase_pipe_kernel, &cfg) == cudaSuccess && nclusters >= 1)
+        if (cudaOccupancyMaxActiveClusters(&nclusters, phase_cluster_kernel, &cfg) == cudaSuccess && nclusters >= 1)
             break;
         cudaGetLastError();
     }
     attr[0].val.clusterDim.x = ncta;
     cfg.gridDim = dim3(njobs * ncta);
-    e = cudaLaunchKernelEx(&cfg, phase_pipe_kernel, jobs_dev);
+    e = cudaLaunchKernelEx(&cfg, phase_cluster_kernel, jobs_dev);
     note_launches(1);
     return e != cudaSuccess ? e : cudaGetLastError();
 }
