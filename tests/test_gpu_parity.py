@@ -247,6 +247,33 @@ def test_frame_dtypes_agree(smip):
         assert np.array_equal(o["flags"], outs[0]["flags"])
 
 
+def test_reused_stack_across_frame_types(smip):
+    """One stack reset between jobs of different frame types -- u8, then u16
+    and f64 (larger elements: its staging buffers are replaced), then u8
+    again (smaller: the buffers are reused) -- gives, job by job, exactly
+    the results of a fresh stack; the reference frame and shift list are
+    allocated with the stack, so no job reallocates them."""
+    from smip_gb300 import synthetic as S
+
+    spec = S.StackSpec(n=64, nframes=70, kind="extended", dtype="uint16", d_over_r0=6.0, bdepth=16, seed=29)
+    fr = S.make_stack(spec)
+    jobs = [(fr[:40] >> 4).astype(np.uint8), fr[10:70], fr[5:50].astype(np.float64), (fr[30:70] >> 4).astype(np.uint8)]
+
+    def results(st, frames):
+        st.push_frames(frames)
+        img, ph, fl, cs = st.finish(20.0)
+        return st.shifts(), st.sum(), st.bispectrum(), img, fl
+
+    with smip.Stack(64, 64, 16, batch_frames=32) as st:
+        for frames in jobs:
+            got = results(st, frames)
+            with smip.Stack(64, 64, 16, batch_frames=32) as fresh:
+                exp = results(fresh, frames)
+            for g, e in zip(got, exp):
+                assert np.array_equal(g, e)
+            st.reset()
+
+
 @pytest.mark.parametrize("dtype", [np.uint8, np.uint16, np.float32, np.float64])
 def test_host_device_and_page_locked_sources_agree(smip, dtype):
     """The same frames pushed from pageable host memory (copied), from
