@@ -299,10 +299,13 @@ def serving_metrics(jobs):
     keep = serve.pin_banks(batched + served + [j for jl in sweep.values() for j in jl])
     shapes = {j.shape for j in batched + served}
     out = {}
+    # one pool of 40 stacks per shape, shared by the two engines (they run one
+    # after the other), so that no run creates a stack (a device allocation
+    # and synchronisation) while it is timed
     eng = serve.Engine(budget_bytes=120e9, max_active=64, workers=32)
-    eng.prewarm(shapes, count=24)
+    eng.prewarm(shapes, count=40)
     eng_m = serve.Engine(budget_bytes=120e9, max_active=64, workers=32, graph=True)
-    eng_m.prewarm(shapes, count=24)
+    eng_m.pool = eng.pool
     serve.run_plain(batched[:3], realtime=False)  # warm the code paths
     eng_m.run(batched[:8], realtime=False)
     runs_s = [eng.run(batched, realtime=False) for _ in range(2)]
