@@ -303,7 +303,7 @@ def serving_metrics(jobs):
     # after the other), so that no run creates a stack (a device allocation
     # and synchronisation) while it is timed
     eng = serve.Engine(budget_bytes=120e9, max_active=64, workers=32)
-    eng.prewarm(shapes, count=40)
+    eng.prewarm(shapes, count=40, reco_radius=lambda shape: 2.0 * shape[2])  # the jobs' radius: 2 x depth
     eng_m = serve.Engine(budget_bytes=120e9, max_active=64, workers=32, graph=True)
     eng_m.pool = eng.pool
     serve.run_plain(batched[:3], realtime=False)  # warm the code paths

@@ -192,6 +192,13 @@ SMIP_GPU_API int smip_stack_reconstruct(smip_stack_t s, double reco_radius, doub
 SMIP_GPU_API int smip_stack_finish(smip_stack_t s, double reco_radius, double* image, double* phases,
                                    unsigned char* flags, double* consistency);
 
+/* Allocates the reconstruction's device buffers and builds its spiral visit
+ * tables for reco_radius ahead of smip_stack_reconstruct / smip_stack_finish
+ * (which otherwise do it on their first call, and again for a new radius):
+ * a serving loop prepares its pooled stacks so that no job allocates device
+ * memory.  Results do not change.  No counterpart in the reference. */
+SMIP_GPU_API int smip_stack_prepare_reco(smip_stack_t s, double reco_radius);
+
 /* Adds src's accumulators into dst (same shape): frame-level sharding of one
  * stack across accumulators (the accumulation is additive).  dst keeps its
  * own reference frame; src must have been created after dst received its

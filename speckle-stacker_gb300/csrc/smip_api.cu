@@ -310,7 +310,9 @@ struct Reco {
         dfree(flags);
         dfree(job);
     }
-    int run(const float2* Bnorm, double radius, int* err, cudaStream_t st)
+    // Buffers and visit tables for radius `radius` (allocated once per stack,
+    // the tables again only when the radius changes).
+    int prepare(double radius, cudaStream_t st)
     {
         const size_t np = (size_t)g.W * g.H;
         if (!phases) {
@@ -386,6 +388,15 @@ struct Reco {
             CUDA_TRY(cudaMalloc(&rlist, sizeof(unsigned short) * kRecentMax * v.size()));
             R = radius;
         }
+        if (mode == 1 && !fring)
+            CUDA_TRY(cudaMalloc(&fring, sizeof(int) * np));
+        return SMIP_OK;
+    }
+    int run(const float2* Bnorm, double radius, int* err, cudaStream_t st)
+    {
+        const size_t np = (size_t)g.W * g.H;
+        if (int rc = prepare(radius, st))
+            return rc;
         CUDA_TRY(cudaMemsetAsync(phases, 0, sizeof(double2) * np, st));
         // the spiral walk's phase map marks a point without a phase by NaN (all bits set)
         CUDA_TRY(cudaMemsetAsync(phf, mode == 1 ? 0 : 0xff, sizeof(float2) * np, st));
@@ -411,8 +422,6 @@ struct Reco {
         j.rlist = rlist;
         CUDA_TRY(cudaMemcpyAsync(job, &j, sizeof(RecoJob), cudaMemcpyHostToDevice, st));
         if (mode == 1) {
-            if (!fring)
-                CUDA_TRY(cudaMalloc(&fring, sizeof(int) * np));
             CUDA_TRY(launch_ring_reco(job, fring, rq, roff, g.W, g.H, st));
         } else {
             CUDA_TRY(launch_phase_reco(job, 1, g.W, g.H, g.De, st));
@@ -1338,6 +1347,27 @@ extern "C" int smip_stack_power(smip_stack_t s, double* out)
     return SMIP_OK;
 }
 
+// The reconstruction's stream (high priority) and its buffers: the
+// normalised bispectrum, the final image and the phase recovery's buffers
+// and visit tables for radius R.
+static int prepare_reco(smip_stack_t s, double R)
+{
+    if (!s->rst) {
+        int least = 0, greatest = 0;
+        CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CUDA_TRY(cudaStreamCreateWithPriority(&s->rst, cudaStreamNonBlocking, greatest));
+        CUDA_TRY(cudaEventCreateWithFlags(&s->ev_reco, cudaEventDisableTiming));
+    }
+    if (!s->Bn)
+        CUDA_TRY(cudaMalloc(&s->Bn, sizeof(float2) * s->g.base_size));
+    if (!s->Z) {
+        CUDA_TRY(cudaMalloc(&s->Z, sizeof(double2) * s->frame_elems()));
+        CUDA_TRY(cudaMalloc(&s->maxbuf, sizeof(double)));
+    }
+    s->reco.g = s->g;
+    return s->reco.prepare(R, s->rst);
+}
+
 static int normalize_bispec(smip_stack_t s, cudaStream_t q)
 {
     if (!s->Bn)
@@ -1370,15 +1400,8 @@ static int stack_reco(smip_stack_t s, double R)
         return rc;
     if (!(R >= 0.0))
         return fail(SMIP_E_INVALID_ARGUMENT, "reco_radius must be >= 0");
-    if (!s->rst) {
-        int least = 0, greatest = 0;
-        CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-        CUDA_TRY(cudaStreamCreateWithPriority(&s->rst, cudaStreamNonBlocking, greatest));
-        CUDA_TRY(cudaEventCreateWithFlags(&s->ev_reco, cudaEventDisableTiming));
-    }
-    if ((rc = normalize_bispec(s, s->rst)))
+    if ((rc = prepare_reco(s, R)) || (rc = normalize_bispec(s, s->rst)))
         return rc;
-    s->reco.g = s->g;
     return s->reco.run(s->Bn, R, s->err, s->rst);
 }
 
@@ -1410,10 +1433,6 @@ extern "C" int smip_stack_finish(smip_stack_t s, double R, double* image, double
     if (!(R > 0.0))
         return fail(SMIP_E_DOMAIN, "WindowFunction aperture size <= 0");
     const size_t n = s->frame_elems();
-    if (!s->Z) {
-        CUDA_TRY(cudaMalloc(&s->Z, sizeof(double2) * n));
-        CUDA_TRY(cudaMalloc(&s->maxbuf, sizeof(double)));
-    }
     const double pnorm = (double)((size_t)s->nframes * n);
     CUDA_TRY(launch_finish(s->P, pnorm, s->reco.phases, 2.0 * R, s->g, s->Z, nullptr, s->maxbuf, s->ctx->tw64, s->rst,
                            s->twW.f64, s->twH.f64));
@@ -1424,6 +1443,20 @@ extern "C" int smip_stack_finish(smip_stack_t s, double R, double* image, double
     if ((rc = s->reco.download(phases, flags, cons, s->st)))
         return rc;
     return check_dev_err(s->err, s->st);
+}
+
+extern "C" int smip_stack_prepare_reco(smip_stack_t s, double reco_radius)
+{
+    int rc = check_stack(s);
+    if (rc)
+        return rc;
+    if (!(reco_radius >= 0.0))
+        return fail(SMIP_E_INVALID_ARGUMENT, "reco_radius must be >= 0");
+    CUDA_TRY(cudaSetDevice(s->device));
+    if ((rc = prepare_reco(s, reco_radius)))
+        return rc;
+    CUDA_TRY(cudaStreamSynchronize(s->rst)); // the visit tables' copies
+    return SMIP_OK;
 }
 
 extern "C" int smip_stack_share_reference(smip_stack_t dst, smip_stack_t src)

@@ -102,6 +102,7 @@ def _load():
         "smip_stack_bispectrum": ([vp, fp], C.c_int),
         "smip_stack_reconstruct": ([vp, C.c_double, dp, ubp, dp], C.c_int),
         "smip_stack_finish": ([vp, C.c_double, dp, dp, ubp, dp], C.c_int),
+        "smip_stack_prepare_reco": ([vp, C.c_double], C.c_int),
         "smip_stack_merge": ([vp, vp], C.c_int),
         "smip_stack_set_kernel_config": ([vp, C.c_int, C.c_int], C.c_int),
         "smip_batch_launch": ([C.POINTER(vp), C.c_long], C.c_int),
@@ -268,6 +269,12 @@ class Stack:
         1 (two); min_part: fewest frames per split part of a last-wave tile
         (0 = 8).  The autotuner picks both ("auto" batch_frames)."""
         _check(_L().smip_stack_set_kernel_config(self._h, int(variant), int(min_part)))
+
+    def prepare_reco(self, reco_radius: float):
+        """Allocates the reconstruction's buffers and visit tables for
+        reco_radius now, so that finish() with that radius allocates nothing
+        (a serving loop prepares its pooled stacks)."""
+        _check(_L().smip_stack_prepare_reco(self._h, float(reco_radius)))
 
     def set_reco_mode(self, mode="spiral"):
         """Phase-recovery estimator: "spiral" (default, the reference's walk)

@@ -193,13 +193,22 @@ class Engine:
         with self._cancel_lock:
             return job_id in self._cancelled
 
-    def prewarm(self, shapes, count: int = 1):
+    def prewarm(self, shapes, count: int = 1, reco_radius=None):
         """Creates ``count`` pooled stacks per (ncols, nrows, bdepth) shape, so
-        that no device allocation happens while jobs are served."""
+        that no device allocation happens while jobs are served.
+        reco_radius (a number, or a function of the shape): the radius the
+        jobs of a shape reconstruct with; the stacks' reconstruction buffers
+        are then allocated here as well."""
         for s in shapes:
             lst = self.pool.setdefault(tuple(s), [])
             while len(lst) < count:
                 lst.append(self.factory(*s))
+            if reco_radius is not None:
+                r = reco_radius(tuple(s)) if callable(reco_radius) else reco_radius
+                for st in lst:
+                    prep = getattr(st, "prepare_reco", None)
+                    if callable(prep):
+                        prep(r)
 
     def _acquire(self, shape):
         lst = self.pool.setdefault(shape, [])

@@ -97,6 +97,26 @@ def test_engine_realtime_respects_arrivals():
         assert r.admitted >= r.arrival - 1e-9 and r.done >= r.admitted
 
 
+def test_prewarm_prepares_reconstructions():
+    """prewarm(reco_radius=...) prepares every pooled stack of a shape for the
+    radius its jobs use (a function of the shape, or one number); stacks
+    without prepare_reco are left as they are."""
+
+    class PreparingStack(FakeStack):
+        def prepare_reco(self, R):
+            self.prepared = R
+
+    eng = serve.Engine(max_active=2, workers=1, stack_factory=PreparingStack)
+    eng.prewarm({(32, 32, 8), (16, 16, 4)}, count=3, reco_radius=lambda shape: 2.0 * shape[2])
+    assert {st.prepared for st in eng.pool[(32, 32, 8)]} == {16.0}
+    assert {st.prepared for st in eng.pool[(16, 16, 4)]} == {8.0} and len(eng.pool[(16, 16, 4)]) == 3
+    eng.prewarm({(16, 16, 4)}, count=4, reco_radius=5.0)
+    assert {st.prepared for st in eng.pool[(16, 16, 4)]} == {5.0} and len(eng.pool[(16, 16, 4)]) == 4
+    plain = serve.Engine(max_active=2, workers=1, stack_factory=FakeStack)
+    plain.prewarm({(16, 16, 4)}, count=2, reco_radius=5.0)  # FakeStack has no prepare_reco
+    assert len(plain.pool[(16, 16, 4)]) == 2
+
+
 def test_engine_pool_reuses_stacks():
     FakeStack.live = 0
     jobs = _jobs(12)
