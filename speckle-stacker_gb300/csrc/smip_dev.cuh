@@ -504,11 +504,6 @@ __device__ __forceinline__ void dsmem_st_relaxed(uint32_t a, int v)
 {
     asm volatile("st.relaxed.cluster.shared::cluster.b32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
-__device__ __forceinline__ void dsmem_st_f4(uint32_t a, float4 v)
-{
-    asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w)
-                 : "memory");
-}
 // Stores into another CTA's shared memory that complete a transaction count
 // on an mbarrier there (st.async): once the barrier's phase completes, a
 // thread of that CTA that waited on it sees the data.
