@@ -229,6 +229,8 @@ public:
                                 r.pm.consistency.data()));
         return r;
     }
+    // buffers and visit tables of finish(reco_radius) ahead of the first call
+    void prepare_reco(double reco_radius) const { check(smip_stack_prepare_reco(handle(), reco_radius)); }
     void write_to_file(const std::string& path) const { check(smip_stack_save_bispectrum(handle(), path.c_str())); }
     void read_from_file(const std::string& path, long nframes = 0)
     {
