@@ -324,6 +324,8 @@ def serving_metrics(jobs):
                       "results_identical": serve.compare_results(res_s, res_p),
                       "peak_jobs_in_flight": eng.peak_active,
                       "served_multi": sm, "frames_per_s_ratio_multi": sm["frames_per_s"] / p["frames_per_s"],
+                      "served_multi_mode": "the finished jobs of a round in groups of 8, each group's bispectrum "
+                                           "work as one persistent launch from a captured CUDA graph",
                       "results_identical_multi": serve.compare_results(res_m, res_p),
                       "served_rings": serve.summarize(*min(runs_r, key=lambda x: x[1]))}
     del eng_m
